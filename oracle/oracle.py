@@ -1,0 +1,302 @@
+"""Python access to the oracles (TEST INFRASTRUCTURE ONLY).
+
+* ``OracleS``  — ctypes wrapper of ``liboracle_s.so`` (nc_oracle.c), the stepped CPU
+  restatement of the NeuCor step.  Used by tests/, ``__graft_entry__.smoke()`` and
+  bench.py's CPU baseline as the checker; never by the product.
+* ``run_reference`` — runs ``_ref/neucor_ref`` (the reference's own src/NeuCor.cpp
+  compiled from its sources by oracle/Makefile) on a scenario.  Only available where
+  the reference tree was present at build time.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_s.so")
+REF_BIN = os.path.join(HERE, "_ref", "neucor_ref")
+NEVER = np.iinfo(np.int32).min
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("run_speed", ctypes.c_float),
+        ("learning_rate", ctypes.c_float),
+        ("presynaptic_trace_decay", ctypes.c_float),
+        ("postsynaptic_trace_decay", ctypes.c_float),
+        ("presynaptic_factor", ctypes.c_float),
+        ("postsynaptic_factor", ctypes.c_float),
+        ("background_firing", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+class Group(ctypes.Structure):
+    _fields_ = [
+        ("first", ctypes.c_int32),
+        ("count", ctypes.c_int32),
+        ("rate_hz", ctypes.c_float),
+        ("correlated", ctypes.c_int32),
+        ("jitter", ctypes.c_int32),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("fires", ctypes.c_int64),
+        ("launched", ctypes.c_int64),
+        ("dropped", ctypes.c_int64),
+        ("arrivals", ctypes.c_int64),
+        ("order_conflicts", ctypes.c_int64),
+        ("first_conflict_step", ctypes.c_int32),
+        ("step", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def build(quiet: bool = True) -> None:
+    """Compile liboracle_s.so (and _ref/neucor_ref when the reference tree exists)."""
+    args = ["make", "-s", "-C", HERE, "all"]
+    subprocess.run(args, check=True, capture_output=quiet)
+    if os.path.isdir("/root/reference/src"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, capture_output=quiet)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        L.ncs_create.restype = P
+        L.ncs_create.argtypes = [ctypes.c_int32, P, ctypes.c_int64, P, P, P, P, ctypes.POINTER(Params)]
+        L.ncs_destroy.argtypes = [P]
+        L.ncs_set_groups.argtypes = [P, ctypes.c_int32, P]
+        L.ncs_set_rates.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+        L.ncs_schedule_fire.argtypes = [P, ctypes.c_int32, P]
+        L.ncs_run.argtypes = [P, ctypes.c_int32, P, P]
+        L.ncs_step.restype = ctypes.c_int32
+        L.ncs_step.argtypes = [P]
+        L.ncs_n_synapses.restype = ctypes.c_int64
+        L.ncs_n_synapses.argtypes = [P]
+        for name in ("ncs_read_potentials", "ncs_read_activity", "ncs_read_last_fire_step",
+                     "ncs_read_weights", "ncs_read_delays"):
+            getattr(L, name).argtypes = [P, P]
+        L.ncs_reset_activities.argtypes = [P]
+        L.ncs_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+        L.ncs_default_params.argtypes = [ctypes.POINTER(Params)]
+        L.ncs_philox4x32_10.argtypes = [P, P, P]
+        L.ncs_input_fires.restype = ctypes.c_int32
+        L.ncs_input_fires.argtypes = [P, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float, ctypes.c_int32, P,
+                                      ctypes.c_int32]
+        L.ncs_background_draws.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_float, ctypes.c_int32, P, P]
+        L.ncs_delay_steps.restype = ctypes.c_int32
+        L.ncs_delay_steps.argtypes = [ctypes.c_float, ctypes.c_float]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().ncs_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def groups_array(groups):
+    arr = (Group * max(1, len(groups)))()
+    for i, g in enumerate(groups):
+        arr[i] = Group(int(g["first"]), int(g["count"]), float(g["rate_hz"]), int(g.get("correlated", 1)),
+                       int(g.get("jitter", 2)))
+    return arr
+
+
+def philox(ctr, key):
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    o = np.zeros(4, dtype=np.uint32)
+    lib().ncs_philox4x32_10(_ptr(c), _ptr(k), _ptr(o))
+    return o
+
+
+class OracleS:
+    """The stepped CPU restatement of NeuCor::run (runAll=true, fixed dt)."""
+
+    def __init__(self, xyz, pre, post, weight, length=None, params: Params | None = None, groups=()):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        self.n = int(self.xyz.shape[0])
+        self.pre = np.ascontiguousarray(pre, dtype=np.int32)
+        self.post = np.ascontiguousarray(post, dtype=np.int32)
+        self.weight = np.ascontiguousarray(weight, dtype=np.float32)
+        self.length = None if length is None else np.ascontiguousarray(length, dtype=np.float32)
+        self.params = params if params is not None else default_params()
+        self.n_input = int(self.pre.shape[0])
+        self.h = lib().ncs_create(self.n, _ptr(self.xyz), self.n_input, _ptr(self.pre), _ptr(self.post),
+                                  _ptr(self.weight), _ptr(self.length), ctypes.byref(self.params))
+        if not self.h:
+            raise ValueError("oracle rejected the network")
+        if groups:
+            g = groups_array(groups)
+            if lib().ncs_set_groups(self.h, len(groups), ctypes.cast(g, ctypes.c_void_p)) != 0:
+                raise ValueError("bad input groups")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().ncs_destroy(h)
+            self.h = None
+
+    def schedule_fire(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        if lib().ncs_schedule_fire(self.h, int(ids.size), _ptr(ids)) != 0:
+            raise ValueError("bad neuron id")
+
+    def set_rates(self, learning_rate, pre_factor, post_factor):
+        lib().ncs_set_rates(self.h, learning_rate, pre_factor, post_factor)
+
+    def run(self, steps: int, raster: bool = False, pots: bool = False):
+        row = (self.n + 7) // 8
+        r = np.zeros((steps, row), dtype=np.uint8) if raster else None
+        p = np.zeros((steps, self.n), dtype=np.float32) if pots else None
+        if lib().ncs_run(self.h, int(steps), _ptr(r), _ptr(p)) != 0:
+            raise ValueError("run failed")
+        return r, p
+
+    @property
+    def step(self) -> int:
+        return int(lib().ncs_step(self.h))
+
+    def potentials(self):
+        o = np.zeros(self.n, dtype=np.float32)
+        lib().ncs_read_potentials(self.h, _ptr(o))
+        return o
+
+    def activity(self):
+        o = np.zeros(self.n, dtype=np.float32)
+        lib().ncs_read_activity(self.h, _ptr(o))
+        return o
+
+    def last_fire_step(self):
+        o = np.zeros(self.n, dtype=np.int32)
+        lib().ncs_read_last_fire_step(self.h, _ptr(o))
+        return o
+
+    def weights(self):
+        o = np.zeros(self.n_input, dtype=np.float32)
+        lib().ncs_read_weights(self.h, _ptr(o))
+        return o
+
+    def delays(self):
+        o = np.zeros(self.n_input, dtype=np.int32)
+        lib().ncs_read_delays(self.h, _ptr(o))
+        return o
+
+    def reset_activities(self):
+        lib().ncs_reset_activities(self.h)
+
+    def stats(self) -> dict:
+        s = Stats()
+        lib().ncs_get_stats(self.h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in Stats._fields_}
+
+
+def input_fires(groups, seed: int, dt: float, t: int):
+    g = groups_array(groups)
+    cap = sum(int(x["count"]) for x in groups) + 1
+    ids = np.zeros(cap, dtype=np.int32)
+    n = lib().ncs_input_fires(ctypes.cast(g, ctypes.c_void_p), len(groups), seed, dt, t, _ptr(ids), cap)
+    return ids[:n]
+
+
+def background_draws(seed: int, n: int, dt: float, counter: int):
+    hit = np.zeros(n, dtype=np.uint8)
+    tgt = np.zeros(n, dtype=np.int32)
+    lib().ncs_background_draws(seed, n, dt, counter, _ptr(hit), _ptr(tgt))
+    return hit.astype(bool), tgt
+
+
+# ------------------------------------------------------------- Oracle-R runner
+MODES = {"canonical": 0, "native": 1, "continuous": 2}
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_BIN) and os.access(REF_BIN, os.X_OK)
+
+
+def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps=100, record_pot=False,
+                  extra_fires=(), checkpoints=(), firers=()):
+    """Run the reference's own simulator on a scenario.  extra_fires: (step, id) pairs
+    requesting a forced fire at that step.  firers: the reference's periodic input
+    firers as dicts (pos, radius, rate_hz, offset_ms), continuous mode only.
+    Returns dict(raster, pots, weights, pot, activity, last_fire)."""
+    if not reference_available():
+        raise RuntimeError("reference harness not built (needs the reference tree)")
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+    n = xyz.shape[0]
+    pre = np.ascontiguousarray(pre, dtype=np.int32)
+    post = np.ascontiguousarray(post, dtype=np.int32)
+    weight = np.ascontiguousarray(weight, dtype=np.float32)
+    s = pre.shape[0]
+    checkpoints = sorted(int(c) for c in checkpoints)
+    with tempfile.TemporaryDirectory() as td:
+        scen = os.path.join(td, "s.bin")
+        outp = os.path.join(td, "o.bin")
+        with open(scen, "wb") as f:
+            f.write(b"NCRF")
+            f.write(struct.pack("<iiq", MODES[mode], n, s))
+            f.write(xyz.tobytes())
+            f.write(pre.tobytes())
+            f.write(post.tobytes())
+            f.write(weight.tobytes())
+            f.write(struct.pack("<6f", params.run_speed, params.learning_rate, params.presynaptic_trace_decay,
+                                params.postsynaptic_trace_decay, params.presynaptic_factor,
+                                params.postsynaptic_factor))
+            f.write(struct.pack("<iQ", params.background_firing, params.seed))
+            f.write(struct.pack("<i", len(groups)))
+            for g in groups:
+                f.write(struct.pack("<iifii", int(g["first"]), int(g["count"]), float(g["rate_hz"]),
+                                    int(g.get("correlated", 1)), int(g.get("jitter", 2))))
+            f.write(struct.pack("<ii", steps, int(bool(record_pot))))
+            f.write(struct.pack("<i", len(extra_fires)))
+            for st, i in extra_fires:
+                f.write(struct.pack("<ii", int(st), int(i)))
+            f.write(struct.pack("<i", len(checkpoints)))
+            f.write(np.asarray(checkpoints, dtype=np.int32).tobytes())
+            f.write(struct.pack("<i", len(firers)))
+            for fr in firers:
+                x, y, z = fr["pos"]
+                f.write(struct.pack("<6f", x, y, z, fr["radius"], fr["rate_hz"], fr.get("offset_ms", 0.0)))
+        subprocess.run([REF_BIN, scen, outp], check=True)
+        data = open(outp, "rb").read()
+    row = (n + 7) // 8
+    off = 0
+    raster = np.frombuffer(data, dtype=np.uint8, count=row * steps, offset=off).reshape(steps, row)
+    off += row * steps
+    pots = None
+    if record_pot:
+        pots = np.frombuffer(data, dtype=np.float32, count=n * steps, offset=off).reshape(steps, n)
+        off += 4 * n * steps
+    ckw = np.frombuffer(data, dtype=np.float32, count=s * len(checkpoints), offset=off).reshape(len(checkpoints), s)
+    off += 4 * s * len(checkpoints)
+    fin = np.frombuffer(data, dtype=np.float32, count=3 * n, offset=off)
+    return {"raster": raster.copy(), "pots": None if pots is None else pots.copy(), "weights": ckw.copy(),
+            "pot": fin[:n].copy(), "activity": fin[n:2 * n].copy(), "last_fire": fin[2 * n:].copy()}
+
+
+def unpack_raster(raster, n):
+    """(steps, ceil(n/8)) bit rows -> (steps, n) bool."""
+    return np.unpackbits(raster, axis=1, bitorder="little")[:, :n].astype(bool)
