@@ -1,0 +1,372 @@
+"""Benchmark of the NeuCor simulation step on GB300.
+
+Workload (the plain single-network GPU configuration): 100,000 neurons uniform in a
+cube at the reference's spawn density, each connected to its 100 nearest neighbours
+(10M synapses), U[0,1) fp32 weights, int16 delays from distance; 200 input neurons in 10
+correlated Poisson groups at 5-40 Hz (+-2-step jitter); STDP on; background firing on.
+One bench step = 1,000 simulation steps (1 s of simulated time at 1 ms per step);
+the default 20 timed steps are the configuration's 20,000-step horizon.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torch.distributed.run);
+the networks do not interact, so there is no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_NEURONS = 100_000
+FANOUT = 100
+SIM_STEPS_PER_STEP = 1000
+N_GROUPS, GROUP_SIZE = 10, 20
+METRIC = "synaptic events/s"
+UNIT = "events/s"
+
+
+def workload_groups():
+    rates = np.linspace(5.0, 40.0, N_GROUPS)
+    return [dict(first=GROUP_SIZE * g, count=GROUP_SIZE, rate_hz=float(rates[g]), correlated=1, jitter=2)
+            for g in range(N_GROUPS)]
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "plain single network: 100k neurons x 100 nearest targets (10M synapses), "
+                       "200 inputs in 10 correlated Poisson groups 5-40 Hz, STDP on, 20,000 steps",
+           "neurons": N_NEURONS, "synapses": N_NEURONS * FANOUT, "sim_steps_per_bench_step": SIM_STEPS_PER_STEP,
+           "dt_ms": 1.0, "l2": "inputs larger than L2 (synapse tables ~350 MB)", "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the neuron-update kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_neuron_step_c2.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_scaled:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def build_network(G, seed):
+    xyz, pre, post, w = G.build_knn(N_NEURONS, FANOUT, 8.0, seed=seed)
+    return xyz, pre, post, w
+
+
+class CpuPort:
+    """The oracle port (the reference's step restated on CPU, single-threaded like the
+    reference) on the same workload; `replicas` independent networks run on as many
+    host threads (the C code runs outside the GIL)."""
+
+    def __init__(self, net_arrays, groups, seed, replicas=1):
+        from oracle import oracle as O
+        xyz, pre, post, w = net_arrays
+        self.sims = [None] * replicas
+
+        def make(r):
+            self.sims[r] = O.OracleS(xyz, pre, post, w, params=O.default_params(seed=seed + r), groups=groups)
+
+        self._parallel(make)
+
+    def _parallel(self, fn):
+        ths = [threading.Thread(target=fn, args=(r,)) for r in range(len(self.sims))]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+
+    def timed(self, sim_steps):
+        """Runs sim_steps on every replica at once; returns (events, wall seconds)."""
+        before = [s.stats()["launched"] for s in self.sims]
+        t0 = time.perf_counter()
+        self._parallel(lambda r: self.sims[r].run(sim_steps))
+        wall = time.perf_counter() - t0
+        return sum(s.stats()["launched"] - b for s, b in zip(self.sims, before)), wall
+
+    def budgeted(self, budget_s, chunk=10, cap=5000):
+        events, wall, steps = 0, 0.0, 0
+        while wall < budget_s and steps < cap:
+            e, dt = self.timed(chunk)
+            events, wall, steps = events + e, wall + dt, steps + chunk
+        return events, wall, steps
+
+
+def host_threads():
+    n = os.cpu_count() or 1
+    try:
+        with open("/proc/meminfo") as fh:
+            avail_kb = next(int(l.split()[1]) for l in fh if l.startswith("MemAvailable"))
+        n = max(1, min(n, int(avail_kb / (1.2 * 1024 * 1024))))  # ~1 GB per 10M-synapse replica
+    except (OSError, StopIteration, ValueError):
+        pass
+    return n
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import neurocorrelation_gb300 as G
+    groups = workload_groups()
+    arrays = build_network(G, seed=1)
+    threads = host_threads()
+    port = CpuPort(arrays, groups, seed=100, replicas=threads)
+    chunk = 10  # one reference-arm step: 10 simulation steps on every replica
+    for _ in range(args.warmup):
+        port.timed(chunk)
+    events, wall = 0, 0.0
+    for _ in range(args.steps):
+        e, dt = port.timed(chunk)
+        events, wall = events + e, wall + dt
+    value = events / wall
+    sample = (f"{threads} replica(s) of the 100k x 100 network on {threads} host thread(s); each step = "
+              f"{chunk} simulation steps per replica after {args.warmup * chunk} warm-up steps "
+              f"(the first {chunk * (args.warmup + args.steps)} steps of the horizon)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local = dist_env()
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    import neurocorrelation_gb300 as G
+
+    G.load_library()
+    if G.device_count() < 1:
+        raise RuntimeError("no CUDA device")
+    G.set_device(local)
+    groups = workload_groups()
+    seed = 1 + rank
+    arrays = build_network(G, seed=seed)
+    net = G.NeuCor.from_arrays(*arrays, params=G.default_params(seed=seed))
+    net.set_input_groups(groups)
+    S = SIM_STEPS_PER_STEP
+
+    def barrier():
+        if pg:
+            import torch
+            t = torch.zeros(1, device="cuda" if torch.cuda.is_available() else "cpu")
+            pg.all_reduce(t)
+
+    net.run(args.warmup * S)
+    net.sync()
+    st0 = net.stats()
+    barrier()
+    with ClockSampler(local) as clk:
+        ms, _ = net.time_steps(args.steps * S)
+    barrier()
+    st1 = net.stats()
+    events = st1["launched"] - st0["launched"]
+    fires = st1["fires"] - st0["fires"]
+    # per-kernel timing pass (outside the timed region)
+    kpass = 200
+    stk0 = net.stats()
+    _, per = net.time_steps(kpass, per_kernel=True)
+    stk1 = net.stats()
+    ev_per_step_k = (stk1["launched"] - stk0["launched"]) / (2 * kpass)
+    # end to end through the public API with host buffers: the step's input definition
+    # in, the step's spike raster and potentials/activities out
+    e2e_steps = min(args.steps, 5)
+    net.record_raster(S)
+    h2d = 0
+    d2h = 0
+    st_e0 = net.stats()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        net.set_input_groups(groups)
+        net.record_raster(S)
+        net.run(S)
+        r = net.raster()
+        pa = net.potAct
+        h2d = 20 * len(groups)
+        d2h = r.nbytes + pa.nbytes
+    net.sync()
+    e2e_wall = time.perf_counter() - t0
+    barrier()
+    st_e1 = net.stats()
+    e2e_events = st_e1["launched"] - st_e0["launched"]
+
+    # aggregate over ranks
+    secs = ms / 1e3
+    tot_events = events
+    e2e_secs = e2e_wall
+    tot_e2e = e2e_events
+    if pg:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([secs, e2e_secs], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        secs, e2e_secs = float(t[0]), float(t[1])
+        c = torch.tensor([tot_events, tot_e2e], dtype=torch.float64, device=dev)
+        pg.all_reduce(c)
+        tot_events, tot_e2e = float(c[0]), float(c[1])
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return 0
+
+    value = tot_events / secs
+    neuron_steps = N_NEURONS * args.steps * S * world / secs
+    peak, peak_kind = measured_peak()
+    n_ms, l_ms = per
+    dominant = "k_neuron_step" if n_ms >= l_ms else "k_spike_launch"
+    # algorithmic bytes (16 per neuron + 14 per synaptic event per step): the neuron
+    # update moves 16 per neuron and 8 per event (weight read+write of plasticity), the
+    # spike launch 6 per event (target index 4 + delay 2)
+    alg_neuron = 16.0 * N_NEURONS + 8.0 * ev_per_step_k
+    alg_launch = 6.0 * ev_per_step_k
+    alg = alg_neuron if dominant == "k_neuron_step" else alg_launch
+    dur = (n_ms if dominant == "k_neuron_step" else l_ms) / 1e3
+    achieved = alg / dur / 1e9
+    traffic = ncu_traffic() if dominant == "k_neuron_step" else None
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        port = CpuPort(arrays, groups, seed=seed, replicas=1)
+        ev, wall, nst = port.budgeted(args.cpu_budget)
+        cpu = {"value": ev / wall, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"first {nst} steps of the same 100k x 100 network on 1 thread ({wall:.1f} s)"}
+    step_alg = (16.0 * N_NEURONS * args.steps * S + 14.0 * events) / secs / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config({"neuron_steps_per_s": neuron_steps, "spikes_per_s": fires * world / secs,
+                                   "mean_rate_hz": fires / (N_NEURONS * args.steps * S / 1000.0),
+                                   "step_pair_alg_gbs": step_alg}),
+        "gpu_launches": 2 * args.steps * S,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "neuron_step_ms": n_ms, "spike_launch_ms": l_ms,
+                     "events_per_step_in_kernel_pass": ev_per_step_k},
+        "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

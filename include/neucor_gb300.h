@@ -1,0 +1,220 @@
+/*
+ * neucor_gb300.h — C ABI of the GB300 NeuroCorrelation simulation step.
+ *
+ * The reference exposes its simulator as the C++ class NeuCor (src/NeuCor.h:36-138)
+ * with no C ABI.  Each entry point below replaces one member of that class (cited
+ * beside it); include/neucor_gb300.hpp wraps them back into a class with the
+ * reference's method names.
+ *
+ * Model.  A handle holds one network resident in GPU memory and advances it in
+ * fixed steps of run_speed ms, every neuron updated every step — the reference's
+ * NeuCor::run with runAll=true (src/NeuCor.cpp:583-617, 595-597).  Spike delays are
+ * rounded to whole steps.  Within a step the reference's per-object rules are
+ * applied in ascending neuron-id order (the stepped model; the parity tests compare
+ * against a CPU restatement of it and against the reference's own code).
+ *
+ * Conventions.  Every function returns NC_OK (0) or a negative NC_ERR_* code; the
+ * message of the calling thread's last error is nc_last_error().  No C++ exception
+ * crosses this boundary.  Arrays are caller-owned host buffers unless stated.  Calls
+ * on one handle must be serialised by the caller; distinct handles may be used from
+ * distinct threads.  Every handle owns one CUDA stream.
+ */
+#ifndef NEUCOR_GB300_H
+#define NEUCOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NC_OK 0
+#define NC_ERR_INVALID (-1)     /* bad argument */
+#define NC_ERR_CUDA (-2)        /* CUDA runtime error (message in nc_last_error) */
+#define NC_ERR_NOMEM (-3)       /* device or host allocation failed */
+#define NC_ERR_UNSUPPORTED (-4) /* reference operation outside the stepped GPU model */
+#define NC_ERR_NODEVICE (-5)    /* no CUDA device */
+#define NC_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up */
+#define NC_ERR_BUDGET (-7)      /* request does not fit the memory budget */
+
+typedef struct nc_net nc_net;
+
+/* Synapse::inhibitory (src/NeuCor.h:290) selects the weight clamp of plasticity
+ * (src/NeuCor.cpp:760-761).  setWeight sets it from the sign (src/NeuCor.cpp:576-579),
+ * but the Synapse copy constructor (src/NeuCor.cpp:487-504) does not copy it, so a
+ * synapse copied when its source's outSynapses vector grows (reserve(5),
+ * src/NeuCor.cpp:374, then capacity doubling) carries an indeterminate flag.
+ *   NC_INHIBITORY_COPY_LOSS  copied synapses are not inhibitory — what the reference
+ *                            shows when the grown vector lands in fresh memory (default);
+ *   NC_INHIBITORY_SIGN       inhibitory = weight < 0 for every synapse.
+ * An explicit flag array given to nc_create overrides the rule. */
+#define NC_INHIBITORY_COPY_LOSS 0
+#define NC_INHIBITORY_SIGN 1
+
+/* Simulation constants.  Field meanings follow NeuCor's public members
+ * (src/NeuCor.h:68-73, defaults src/NeuCor.cpp:18-29). */
+typedef struct {
+    float run_speed;                /* NeuCor::runSpeed: ms per step; fixed for the handle's life */
+    float learning_rate;            /* NeuCor::learningRate */
+    float presynaptic_trace_decay;  /* copied into each Synapse at construction (src/NeuCor.cpp:464) */
+    float postsynaptic_trace_decay; /* copied into each Neuron at construction (src/NeuCor.cpp:369) */
+    float presynaptic_factor;       /* NeuCor::presynapticFactor */
+    float postsynaptic_factor;      /* NeuCor::postsynapticFactor */
+    int32_t background_firing;      /* 1: random background fires every step (src/NeuCor.cpp:604-607); 0: off */
+    int32_t inhibitory_rule;        /* NC_INHIBITORY_* below */
+    uint64_t seed;                  /* key of the counter-based draws (background, inputs) */
+} nc_params;
+
+/* A group of input neurons driven by Poisson spike trains.  Members are the
+ * neurons first .. first+count-1.  Correlated groups share one source whose every
+ * event reaches each member jittered by a uniform +-jitter steps; independent
+ * groups give each member its own train.  A member's spike is a forced fire
+ * request (Neuron::scheduleFire, src/NeuCor.cpp:658-661, 682-686). */
+typedef struct {
+    int32_t first;
+    int32_t count;
+    float rate_hz;
+    int32_t correlated;
+    int32_t jitter;
+} nc_group;
+
+/* Counters of a handle since creation. */
+typedef struct {
+    int64_t steps;     /* steps simulated */
+    int64_t fires;     /* neuron spikes */
+    int64_t launched;  /* synaptic events: spikes accepted by a synapse (src/NeuCor.cpp:727-738) */
+    int64_t dropped;   /* spikes a busy synapse refused (src/NeuCor.cpp:728) */
+} nc_stats;
+
+/* Render snapshot of one synapse: NeuCor::SynapseSnapshot (src/NeuCor.h:45-54,
+ * src/NeuCor.cpp:115-134). */
+typedef struct {
+    int32_t from_id;
+    int32_t to_id;
+    float weight;
+    float pre_potential;   /* Synapse::getPrePot, src/NeuCor.cpp:551-558 */
+    float post_potential;  /* Synapse::getPostPot, src/NeuCor.cpp:560-567 */
+    int32_t inhibitory;
+} nc_synapse_snapshot;
+
+/* ---------------------------------------------------------------- errors */
+const char* nc_last_error(void);
+const char* nc_version(void);
+/* Number of usable CUDA devices (0 on a machine without a GPU). */
+int nc_device_count(int* count);
+/* Makes `device` the calling thread's current device; nc_create places a network on
+ * the current device. */
+int nc_set_device(int device);
+
+/* ------------------------------------------------------------ lifecycle */
+/* Defaults of NeuCor::NeuCor (src/NeuCor.cpp:18-29); background on, seed 0. */
+int nc_default_params(nc_params* out);
+
+/* Builds a network from explicit neurons and synapses on the current CUDA device.
+ * Replaces NeuCor(0) + createNeuron(position) per neuron + createSynapse(to, from,
+ * weight) per synapse, in the given order (src/NeuCor.cpp:17-42, 154-195).  A repeated
+ * (from, to) pair keeps its first weight, as createSynapse does.  syn_length may be
+ * NULL: lengths are then coord3::getDist of the endpoint positions (src/NeuCor.h:16-18,
+ * src/NeuCor.cpp:477-479).  A spike takes length*2 ms (src/NeuCor.cpp:485,733), rounded
+ * to whole steps, at least one.  syn_inhibitory may be NULL (flags then follow
+ * params->inhibitory_rule). */
+int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int32_t* syn_from,
+              const int32_t* syn_to, const float* syn_weight, const float* syn_length,
+              const uint8_t* syn_inhibitory, const nc_params* params, nc_net** out);
+/* Frees the handle and its device memory (NeuCor::~NeuCor, src/NeuCor.cpp:44). */
+int nc_destroy(nc_net* net);
+
+/* Poisson input groups (replaces the role of NeuCor::setInputRateArray,
+ * src/NeuCor.cpp:46-64, with the correlated trains of the benchmark workloads). */
+int nc_set_input_groups(nc_net* net, int32_t n_groups, const nc_group* groups);
+/* Periodic input firers with the reference's rates, positions and radii
+ * (NeuCor::setInputRateArray + InputFirer, src/NeuCor.cpp:46-64, 305-345) —
+ * not implemented in the stepped model yet. */
+int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
+                            const float* radius);
+/* Runtime-settable rates (NeuCor::learningRate, presynapticFactor,
+ * postsynapticFactor are read live by the reference, src/NeuCor.cpp:757-758). */
+int nc_set_rates(nc_net* net, float learning_rate, float presynaptic_factor, float postsynaptic_factor);
+/* Forced fire requests for the next step (Neuron::scheduleFire, src/NeuCor.cpp:658-661). */
+int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* neuron_ids);
+
+/* ------------------------------------------------------------------ run */
+/* Advances n_steps steps (NeuCor::run called n_steps times, src/NeuCor.cpp:583-617).
+ * Asynchronous on the handle's stream; read-backs synchronise. */
+int nc_run(nc_net* net, int32_t n_steps);
+/* Waits for the handle's queued work. */
+int nc_sync(nc_net* net);
+/* NeuCor::getTime (src/NeuCor.cpp:225): simulated ms, accumulated in float like the
+ * reference. */
+int nc_get_time(nc_net* net, float* ms);
+int nc_get_step(nc_net* net, int64_t* step);
+int nc_get_counts(nc_net* net, int32_t* n_neurons, int64_t* n_synapses);
+
+/* Records the spike raster of the next max_steps steps into device memory
+ * (replaces the renderer's per-frame scan of Neuron::lastFire,
+ * src/NeuCor_Renderer.cpp:1841-1870).  max_steps = 0 stops recording. */
+int nc_record_raster(nc_net* net, int32_t max_steps);
+/* Copies the recorded raster: steps rows of ceil(N/8) bytes, bit j of row r set
+ * when neuron j fired at the r-th recorded step.  *steps receives the row count. */
+int nc_read_raster(nc_net* net, uint8_t* out, int64_t capacity_bytes, int32_t* steps);
+
+/* ------------------------------------------------------------ read-back */
+/* NeuCor::potAct (src/NeuCor.h:105): potential, activity interleaved, 2*N floats. */
+int nc_read_potact(nc_net* net, float* out_2n);
+int nc_read_potentials(nc_net* net, float* out_n);
+/* NeuCor::positions (src/NeuCor.h:104), 3*N floats. */
+int nc_read_positions(nc_net* net, float* out_3n);
+/* Neuron::lastFire (src/NeuCor.h:226) in ms, NaN when the neuron never fired. */
+int nc_read_last_fire(nc_net* net, float* out_n);
+/* Synapse weights (Synapse::getWeight, src/NeuCor.cpp:572) in the order the
+ * synapses were given to nc_create; NaN for ignored duplicates. */
+int nc_read_weights(nc_net* net, float* out_s);
+/* Delay of each synapse in steps, same order; -1 for ignored duplicates. */
+int nc_read_delays(nc_net* net, int32_t* out_s);
+/* Synapse::inhibitory of each synapse, same order: 0/1, 255 for ignored duplicates. */
+int nc_read_inhibitory(nc_net* net, uint8_t* out_s);
+/* NeuCor::getSynapseSnapshots (src/NeuCor.cpp:115-134), one entry per kept
+ * synapse in source-then-creation order (the reference's outSynapses order). */
+int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t capacity, int64_t* count);
+/* NeuCor::resetActivities (src/NeuCor.cpp:233-235). */
+int nc_reset_activities(nc_net* net);
+int nc_get_stats(nc_net* net, nc_stats* out);
+
+/* Topology mutation after construction (NeuCor::deleteNeuron / deleteSynapse /
+ * queFlip, src/NeuCor.cpp:230-232, 265-296) is outside the GPU model:
+ * these return NC_ERR_UNSUPPORTED. */
+int nc_delete_synapse(nc_net* net, int32_t from_id, int32_t to_id);
+int nc_delete_neuron(nc_net* net, int32_t id);
+
+/* ------------------------------------------------------ network builders */
+/* Host-side construction helpers (no GPU needed).
+ *
+ * nc_build_knn: n neurons uniform in a cube of side (n/density)^(1/3), each
+ * connected to its k nearest neighbours (ties by index), weights uniform [0,1),
+ * all drawn from the counter-based generator keyed by seed.  Outputs: xyz (3n),
+ * from/to/weight (n*k).  Lengths follow coord3::getDist (src/NeuCor.h:16-18). */
+int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, float* xyz, int32_t* syn_from,
+                 int32_t* syn_to, float* syn_weight);
+/* nc_build_reference_random: the reference constructor NeuCor(n) (src/NeuCor.cpp:17-42):
+ * sphere placement (src/NeuCor.cpp:154-170) and radius-1 connection of every ordered
+ * pair (src/NeuCor.cpp:418-444) with weights rand()*0.8+0.2, 20% negated
+ * (src/NeuCor.cpp:471-473), drawing from the C library's rand() in the reference's
+ * order — so after srand(s) it builds the network the reference builds after srand(s).
+ * Pass NULL outputs to get *n_synapses first. */
+int nc_build_reference_random(int32_t n, float* xyz, int32_t* syn_from, int32_t* syn_to, float* syn_weight,
+                              int64_t capacity, int64_t* n_synapses);
+
+/* Philox4x32-10 (Salmon et al., SC'11), the counter-based generator behind every draw. */
+int nc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Times n_steps of the handle's step kernels with CUDA events on its stream;
+ * *ms receives the elapsed device time, *kernel_ms (may be NULL) two entries:
+ * the mean time of one neuron-update and one spike-launch launch over a separate
+ * instrumented pass of min(n_steps, 200) steps. */
+int nc_time_steps(nc_net* net, int32_t n_steps, float* ms, float* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,490 @@
+"""NeuroCorrelation simulation step on GB300 — Python binding of the C ABI.
+
+``NeuCor`` mirrors the reference's C++ class (src/NeuCor.h:36-138): construct a
+network from neuron positions and synapses (or with ``createNeuron`` /
+``createSynapse`` before the first ``run``), set inputs, ``run()`` it, read back
+potentials, spikes and weights.  Every call goes through ``libneucor_gb300.so``
+(include/neucor_gb300.h); there is no CPU fallback — without the library or a CUDA
+device, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+__all__ = ["NeuCor", "Params", "Group", "NeuCorError", "load_library", "library_path", "build_knn",
+           "build_reference_random", "philox4x32_10", "device_count"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_lib", "libneucor_gb300.so")
+
+NC_OK = 0
+_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "no CUDA device",
+           -6: "device wait timed out", -7: "over memory budget"}
+
+
+class NeuCorError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERRORS.get(code, 'error')} ({code}): {message}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """nc_params: NeuCor's public simulation members (src/NeuCor.h:68-73)."""
+    _fields_ = [
+        ("run_speed", ctypes.c_float),
+        ("learning_rate", ctypes.c_float),
+        ("presynaptic_trace_decay", ctypes.c_float),
+        ("postsynaptic_trace_decay", ctypes.c_float),
+        ("presynaptic_factor", ctypes.c_float),
+        ("postsynaptic_factor", ctypes.c_float),
+        ("background_firing", ctypes.c_int32),
+        ("inhibitory_rule", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+class Group(ctypes.Structure):
+    _fields_ = [("first", ctypes.c_int32), ("count", ctypes.c_int32), ("rate_hz", ctypes.c_float),
+                ("correlated", ctypes.c_int32), ("jitter", ctypes.c_int32)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int64), ("fires", ctypes.c_int64), ("launched", ctypes.c_int64),
+                ("dropped", ctypes.c_int64)]
+
+
+class SynapseSnapshotC(ctypes.Structure):
+    _fields_ = [("from_id", ctypes.c_int32), ("to_id", ctypes.c_int32), ("weight", ctypes.c_float),
+                ("pre_potential", ctypes.c_float), ("post_potential", ctypes.c_float), ("inhibitory", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads libneucor_gb300.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(_LIB)
+    P, I32, I64, F = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+    sigs = {
+        "nc_last_error": ([], ctypes.c_char_p), "nc_version": ([], ctypes.c_char_p),
+        "nc_device_count": ([P], I32), "nc_default_params": ([P], I32), "nc_set_device": ([I32], I32),
+        "nc_create": ([I32, P, I64, P, P, P, P, P, P, P], I32), "nc_destroy": ([P], I32),
+        "nc_set_input_groups": ([P, I32, P], I32), "nc_set_input_rate_array": ([P, P, ctypes.c_uint32, P, P], I32),
+        "nc_set_rates": ([P, F, F, F], I32), "nc_schedule_fire": ([P, I32, P], I32),
+        "nc_run": ([P, I32], I32), "nc_sync": ([P], I32), "nc_get_time": ([P, P], I32),
+        "nc_get_step": ([P, P], I32), "nc_get_counts": ([P, P, P], I32), "nc_record_raster": ([P, I32], I32),
+        "nc_read_raster": ([P, P, I64, P], I32), "nc_read_potact": ([P, P], I32),
+        "nc_read_potentials": ([P, P], I32), "nc_read_positions": ([P, P], I32),
+        "nc_read_last_fire": ([P, P], I32), "nc_read_weights": ([P, P], I32), "nc_read_delays": ([P, P], I32),
+        "nc_read_inhibitory": ([P, P], I32),
+        "nc_read_synapse_snapshots": ([P, P, I64, P], I32), "nc_reset_activities": ([P], I32),
+        "nc_get_stats": ([P, P], I32), "nc_delete_synapse": ([P, I32, I32], I32),
+        "nc_delete_neuron": ([P, I32], I32),
+        "nc_build_knn": ([I32, I32, F, ctypes.c_uint64, P, P, P, P], I32),
+        "nc_build_reference_random": ([I32, P, P, P, P, I64, P], I32),
+        "nc_philox4x32_10": ([P, P, P], I32), "nc_time_steps": ([P, I32, P, P], I32),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != NC_OK:
+        raise NeuCorError(rc, load_library().nc_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_count() -> int:
+    c = ctypes.c_int32(0)
+    _check(load_library().nc_device_count(ctypes.byref(c)))
+    return int(c.value)
+
+
+def set_device(device: int) -> None:
+    _check(load_library().nc_set_device(int(device)))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    _check(load_library().nc_default_params(ctypes.byref(p)))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def philox4x32_10(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    o = np.zeros(4, dtype=np.uint32)
+    _check(load_library().nc_philox4x32_10(_p(c), _p(k), _p(o)))
+    return o
+
+
+def build_knn(n: int, k: int, density: float = 8.0, seed: int = 0):
+    """n neurons uniform in a cube at the reference's spawn density (src/NeuCor.cpp:155),
+    each connected to its k nearest neighbours; weights uniform [0, 1)."""
+    xyz = np.zeros((n, 3), dtype=np.float32)
+    pre = np.zeros(n * k, dtype=np.int32)
+    post = np.zeros(n * k, dtype=np.int32)
+    w = np.zeros(n * k, dtype=np.float32)
+    _check(load_library().nc_build_knn(n, k, density, seed, _p(xyz), _p(pre), _p(post), _p(w)))
+    return xyz, pre, post, w
+
+
+def build_reference_random(n: int, seed: int):
+    """The network NeuCor(n) builds after srand(seed) (src/NeuCor.cpp:17-42)."""
+    libc = ctypes.CDLL(None)
+    libc.srand(ctypes.c_uint(seed))
+    L = load_library()
+    cnt = ctypes.c_int64(0)
+    _check(L.nc_build_reference_random(n, None, None, None, None, 0, ctypes.byref(cnt)))
+    libc.srand(ctypes.c_uint(seed))
+    xyz = np.zeros((n, 3), dtype=np.float32)
+    s = cnt.value
+    pre = np.zeros(s, dtype=np.int32)
+    post = np.zeros(s, dtype=np.int32)
+    w = np.zeros(s, dtype=np.float32)
+    _check(L.nc_build_reference_random(n, _p(xyz), _p(pre), _p(post), _p(w), s, ctypes.byref(cnt)))
+    return xyz, pre, post, w
+
+
+@dataclass
+class NeuronSnapshot:       # NeuCor::NeuronSnapshot (src/NeuCor.h:38-43)
+    id: int
+    position: tuple
+    potential: float
+    activity: float
+
+
+@dataclass
+class SynapseSnapshot:      # NeuCor::SynapseSnapshot (src/NeuCor.h:45-54)
+    fromID: int
+    toID: int
+    from_: tuple
+    to: tuple
+    weight: float
+    prePotential: float
+    postPotential: float
+    inhibitory: bool
+
+
+class NeuCor:
+    """GPU-resident NeuroCorrelation network with the reference's method names.
+
+    ``NeuCor(0)`` followed by ``createNeuron`` / ``createSynapse`` builds a network the
+    way the reference's presets do (src/main.cpp:162-189); the network is uploaded at
+    the first ``run``.  ``NeuCor.from_arrays`` builds it from positions and synapse
+    arrays in one call.
+    """
+
+    def __init__(self, n_neurons: int = 0, params: Params | None = None, seed: int | None = None):
+        self._lib = load_library()
+        self._h = None
+        self._params = params if params is not None else default_params()
+        if seed is not None:
+            self._params.seed = seed
+        self._pos: list = []
+        self._syn: list = []
+        self._groups: list = []
+        self._pending_fires: list = []
+        if n_neurons:
+            xyz, pre, post, w = build_reference_random(n_neurons, int(self._params.seed) & 0xffffffff)
+            self._pos = [tuple(map(float, p)) for p in xyz]
+            self._syn = list(zip(pre.tolist(), post.tolist(), w.tolist()))
+
+    # ------------------------------------------------------------ construction
+    @classmethod
+    def from_arrays(cls, xyz, pre, post, weight, length=None, params: Params | None = None, inhibitory=None, **kw):
+        self = cls(0, params=params)
+        for k, v in kw.items():
+            setattr(self._params, k, v)
+        self._materialize(xyz, pre, post, weight, length, inhibitory)
+        return self
+
+    def createNeuron(self, position):
+        """NeuCor::createNeuron (src/NeuCor.cpp:154-186), before the first run."""
+        if self._h is not None:
+            raise NeuCorError(-4, "the network is on the GPU; topology is fixed after the first run")
+        self._pos.append(tuple(float(v) for v in position))
+
+    def createSynapse(self, toID: int, fromID: int, weight: float):
+        """NeuCor::createSynapse (src/NeuCor.cpp:187-195), before the first run."""
+        if self._h is not None:
+            raise NeuCorError(-4, "the network is on the GPU; topology is fixed after the first run")
+        self._syn.append((int(fromID), int(toID), float(weight)))
+
+    def _materialize(self, xyz=None, pre=None, post=None, weight=None, length=None, inhibitory=None):
+        if xyz is None:
+            xyz = np.asarray(self._pos, dtype=np.float32).reshape(-1, 3)
+            if self._syn:
+                pre, post, weight = (np.asarray(c) for c in zip(*self._syn))
+            else:
+                pre = post = np.zeros(0, np.int32)
+                weight = np.zeros(0, np.float32)
+        self._xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        self._pre = np.ascontiguousarray(pre, dtype=np.int32)
+        self._post = np.ascontiguousarray(post, dtype=np.int32)
+        self._w0 = np.ascontiguousarray(weight, dtype=np.float32)
+        ln = None if length is None else np.ascontiguousarray(length, dtype=np.float32)
+        inh = None if inhibitory is None else np.ascontiguousarray(inhibitory, dtype=np.uint8)
+        h = ctypes.c_void_p()
+        _check(self._lib.nc_create(self._xyz.shape[0], _p(self._xyz), self._pre.shape[0], _p(self._pre),
+                                   _p(self._post), _p(self._w0), _p(ln), _p(inh), ctypes.byref(self._params),
+                                   ctypes.byref(h)))
+        self._h = h
+        self.n = int(self._xyz.shape[0])
+        self.n_input_synapses = int(self._pre.shape[0])
+        if self._groups:
+            self._apply_groups()
+        if self._pending_fires:
+            self.schedule_fire(self._pending_fires)
+            self._pending_fires = []
+
+    def _handle(self):
+        if self._h is None:
+            self._materialize()
+        return self._h
+
+    def close(self):
+        if self._h is not None:
+            self._lib.nc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ inputs
+    def set_input_groups(self, groups):
+        """Poisson input groups: dicts with first, count, rate_hz, correlated, jitter."""
+        self._groups = list(groups)
+        if self._h is not None:
+            self._apply_groups()
+
+    def _apply_groups(self):
+        arr = (Group * max(1, len(self._groups)))()
+        for i, g in enumerate(self._groups):
+            arr[i] = Group(int(g["first"]), int(g["count"]), float(g["rate_hz"]), int(g.get("correlated", 1)),
+                           int(g.get("jitter", 2)))
+        _check(self._lib.nc_set_input_groups(self._h, len(self._groups), ctypes.cast(arr, ctypes.c_void_p)))
+
+    def setInputRateArray(self, inputs, inputCount=None, inputPositions=None, inputRadius=None):
+        """NeuCor::setInputRateArray (src/NeuCor.cpp:46-64): periodic firers are not in the
+        stepped GPU model yet; raises NeuCorError(unsupported)."""
+        rates = np.ascontiguousarray(inputs, dtype=np.float32)
+        _check(self._lib.nc_set_input_rate_array(self._handle(), _p(rates), rates.size, None, None))
+
+    def schedule_fire(self, ids):
+        """Neuron::scheduleFire for the next step (src/NeuCor.cpp:658-661)."""
+        if self._h is None:
+            self._pending_fires.extend(int(i) for i in np.atleast_1d(ids))
+            return
+        ids = np.ascontiguousarray(np.atleast_1d(ids), dtype=np.int32)
+        _check(self._lib.nc_schedule_fire(self._h, ids.size, _p(ids)))
+
+    # -------------------------------------------------------------- parameters
+    @property
+    def runSpeed(self) -> float:
+        return float(self._params.run_speed)
+
+    @runSpeed.setter
+    def runSpeed(self, v: float):
+        if self._h is not None and float(v) != self.runSpeed:
+            raise NeuCorError(-4, "runSpeed is fixed once the network is on the GPU")
+        self._params.run_speed = float(v)
+
+    @property
+    def runAll(self) -> bool:
+        return True  # every neuron is updated every step
+
+    @runAll.setter
+    def runAll(self, v: bool):
+        if not v:
+            raise NeuCorError(-4, "the GPU step updates every neuron every step (runAll=true)")
+
+    def _rate(self, name, v=None):
+        if v is None:
+            return float(getattr(self._params, name))
+        setattr(self._params, name, float(v))
+        if self._h is not None:
+            p = self._params
+            _check(self._lib.nc_set_rates(self._h, p.learning_rate, p.presynaptic_factor, p.postsynaptic_factor))
+
+    learningRate = property(lambda s: s._rate("learning_rate"), lambda s, v: s._rate("learning_rate", v))
+    presynapticFactor = property(lambda s: s._rate("presynaptic_factor"),
+                                 lambda s, v: s._rate("presynaptic_factor", v))
+    postsynapticFactor = property(lambda s: s._rate("postsynaptic_factor"),
+                                  lambda s, v: s._rate("postsynaptic_factor", v))
+
+    @property
+    def presynapticTraceDecay(self) -> float:
+        return float(self._params.presynaptic_trace_decay)
+
+    @presynapticTraceDecay.setter
+    def presynapticTraceDecay(self, v):
+        if self._h is not None:
+            raise NeuCorError(-4, "trace decays are copied into synapses at construction")
+        self._params.presynaptic_trace_decay = float(v)
+
+    @property
+    def postsynapticTraceDecay(self) -> float:
+        return float(self._params.postsynaptic_trace_decay)
+
+    @postsynapticTraceDecay.setter
+    def postsynapticTraceDecay(self, v):
+        if self._h is not None:
+            raise NeuCorError(-4, "trace decays are copied into neurons at construction")
+        self._params.postsynaptic_trace_decay = float(v)
+
+    # --------------------------------------------------------------------- run
+    def run(self, steps: int = 1):
+        """NeuCor::run (src/NeuCor.cpp:583-617), `steps` times."""
+        _check(self._lib.nc_run(self._handle(), int(steps)))
+
+    def sync(self):
+        _check(self._lib.nc_sync(self._handle()))
+
+    def getTime(self) -> float:
+        v = ctypes.c_float()
+        _check(self._lib.nc_get_time(self._handle(), ctypes.byref(v)))
+        return float(v.value)
+
+    @property
+    def step(self) -> int:
+        v = ctypes.c_int64()
+        _check(self._lib.nc_get_step(self._handle(), ctypes.byref(v)))
+        return int(v.value)
+
+    def getNeuronCount(self) -> int:
+        if self._h is None:
+            return len(self._pos)
+        n = ctypes.c_int32()
+        _check(self._lib.nc_get_counts(self._h, ctypes.byref(n), None))
+        return int(n.value)
+
+    def record_raster(self, max_steps: int):
+        _check(self._lib.nc_record_raster(self._handle(), int(max_steps)))
+
+    def raster(self):
+        """Recorded spike rows: (steps, ceil(N/8)) bytes, bit j = neuron j fired."""
+        h = self._handle()
+        steps = ctypes.c_int32()
+        _check(self._lib.nc_read_raster(h, None, 0, ctypes.byref(steps)))
+        out = np.zeros((steps.value, (self.n + 7) // 8), dtype=np.uint8)
+        _check(self._lib.nc_read_raster(h, _p(out), out.size, ctypes.byref(steps)))
+        return out
+
+    # --------------------------------------------------------------- read-back
+    @property
+    def potAct(self):
+        """NeuCor::potAct (src/NeuCor.h:105): [potential, activity] per neuron."""
+        out = np.zeros(2 * self.getNeuronCount(), dtype=np.float32)
+        _check(self._lib.nc_read_potact(self._handle(), _p(out)))
+        return out
+
+    def potentials(self):
+        out = np.zeros(self.getNeuronCount(), dtype=np.float32)
+        _check(self._lib.nc_read_potentials(self._handle(), _p(out)))
+        return out
+
+    @property
+    def positions(self):
+        out = np.zeros((self.getNeuronCount(), 3), dtype=np.float32)
+        _check(self._lib.nc_read_positions(self._handle(), _p(out)))
+        return out
+
+    def lastFire(self):
+        out = np.zeros(self.getNeuronCount(), dtype=np.float32)
+        _check(self._lib.nc_read_last_fire(self._handle(), _p(out)))
+        return out
+
+    def weights(self):
+        h = self._handle()
+        out = np.zeros(self.n_input_synapses, dtype=np.float32)
+        _check(self._lib.nc_read_weights(h, _p(out)))
+        return out
+
+    def inhibitory(self):
+        h = self._handle()
+        out = np.zeros(self.n_input_synapses, dtype=np.uint8)
+        _check(self._lib.nc_read_inhibitory(h, _p(out)))
+        return out
+
+    def delays(self):
+        h = self._handle()
+        out = np.zeros(self.n_input_synapses, dtype=np.int32)
+        _check(self._lib.nc_read_delays(h, _p(out)))
+        return out
+
+    def synapse_snapshot_array(self):
+        h = self._handle()
+        cnt = ctypes.c_int64()
+        _check(self._lib.nc_read_synapse_snapshots(h, None, 0, ctypes.byref(cnt)))
+        arr = (SynapseSnapshotC * max(1, cnt.value))()
+        _check(self._lib.nc_read_synapse_snapshots(h, ctypes.cast(arr, ctypes.c_void_p), cnt.value,
+                                                   ctypes.byref(cnt)))
+        return arr[:cnt.value]
+
+    def getNeuronSnapshots(self):
+        """NeuCor::getNeuronSnapshots (src/NeuCor.cpp:99-113)."""
+        pa = self.potAct
+        pos = self.positions
+        return [NeuronSnapshot(i, tuple(map(float, pos[i])), float(pa[2 * i]), float(pa[2 * i + 1]))
+                for i in range(self.getNeuronCount())]
+
+    def getSynapseSnapshots(self):
+        """NeuCor::getSynapseSnapshots (src/NeuCor.cpp:115-134)."""
+        pos = self.positions
+        return [SynapseSnapshot(s.from_id, s.to_id, tuple(map(float, pos[s.from_id])), tuple(map(float, pos[s.to_id])),
+                                float(s.weight), float(s.pre_potential), float(s.post_potential), bool(s.inhibitory))
+                for s in self.synapse_snapshot_array()]
+
+    def resetActivities(self):
+        _check(self._lib.nc_reset_activities(self._handle()))
+
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(self._lib.nc_get_stats(self._handle(), ctypes.byref(s)))
+        return {f: int(getattr(s, f)) for f, _ in _Stats._fields_}
+
+    def time_steps(self, steps: int, per_kernel: bool = False):
+        """Runs `steps` steps timed with CUDA events; returns (ms, [neuron_ms, launch_ms] or None)."""
+        ms = ctypes.c_float()
+        km = (ctypes.c_float * 2)() if per_kernel else None
+        _check(self._lib.nc_time_steps(self._handle(), int(steps), ctypes.byref(ms),
+                                       ctypes.cast(km, ctypes.c_void_p) if km is not None else None))
+        return float(ms.value), (list(km) if km is not None else None)
+
+    def deleteSynapse(self, fromID, toID):
+        _check(self._lib.nc_delete_synapse(self._handle(), int(fromID), int(toID)))
+
+    def deleteNeuron(self, ID):
+        _check(self._lib.nc_delete_neuron(self._handle(), int(ID)))
+
+
+def _nan_to_none(v):
+    return None if (isinstance(v, float) and math.isnan(v)) else v

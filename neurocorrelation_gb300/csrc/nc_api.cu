@@ -1,0 +1,465 @@
+// nc_api.cu — the C ABI of include/neucor_gb300.h for a single network.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "nc_pool.h"
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+// AP_RENDER_BEHAVIOUR (src/NeuCor.cpp:547-550)
+float render_behaviour(float val)
+{
+    val = (float)fmin(fmax((double)val, 0.0), 0.7);
+    if (val < 0.5) val = (float)(8.0 * 1000.0 * powf((float)(val / 5.0), 3.0f));
+    else {
+        const float x = (float)(3.5 - 5 * val);
+        val = (float)(8.0 * (x * x));
+    }
+    return val;
+}
+}  // namespace
+
+struct nc_net {
+    nc::NetHost host;
+    nc::Engine eng;
+    int64_t step = 0;      // completed steps
+    float time = 0.0f;     // NeuCor::currentTime, accumulated per step
+    uint32_t* d_raster = nullptr;
+    int32_t raster_cap = 0;
+    int32_t raster_t0 = 0;
+    ~nc_net()
+    {
+        if (d_raster) cudaFree(d_raster);
+    }
+};
+
+#define NC_NEED(net)                                                  \
+    do {                                                              \
+        if (!(net)) return fail(NC_ERR_INVALID, "null handle");       \
+        cudaError_t e_ = cudaSetDevice((net)->eng.device);            \
+        if (e_ != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("cudaSetDevice", e_)); \
+    } while (0)
+
+#define NC_TRY(expr)                              \
+    do {                                          \
+        std::string err_;                         \
+        int rc_ = (expr);                         \
+        if (rc_ != NC_OK) return fail(rc_, err_); \
+    } while (0)
+
+// NC_TRY needs `err_` visible inside expr
+#define NC_CALL(obj, method, ...)                                  \
+    do {                                                           \
+        std::string err_;                                          \
+        int rc_ = (obj).method(__VA_ARGS__, err_);                 \
+        if (rc_ != NC_OK) return fail(rc_, err_);                  \
+    } while (0)
+#define NC_CALL0(obj, method)                                      \
+    do {                                                           \
+        std::string err_;                                          \
+        int rc_ = (obj).method(err_);                              \
+        if (rc_ != NC_OK) return fail(rc_, err_);                  \
+    } while (0)
+
+extern "C" {
+
+const char* nc_last_error(void) { return g_err.c_str(); }
+const char* nc_version(void) { return "neurocorrelation_gb300 0.1 (sm_103a)"; }
+
+int nc_device_count(int* count)
+{
+    if (!count) return fail(NC_ERR_INVALID, "null count");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    *count = (e == cudaSuccess) ? c : 0;
+    return NC_OK;
+}
+
+int nc_set_device(int device)
+{
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("cudaSetDevice", e));
+    return NC_OK;
+}
+
+int nc_default_params(nc_params* out)
+{
+    if (!out) return fail(NC_ERR_INVALID, "null params");
+    std::memset(out, 0, sizeof(*out));
+    out->run_speed = 1.0f;               // src/NeuCor.cpp:18
+    out->learning_rate = 1.0f;           // src/NeuCor.cpp:24
+    out->presynaptic_trace_decay = 0.75f;
+    out->postsynaptic_trace_decay = 0.65f;
+    out->presynaptic_factor = 0.13f;
+    out->postsynaptic_factor = 0.30f;
+    out->background_firing = 1;
+    out->inhibitory_rule = NC_INHIBITORY_COPY_LOSS;
+    out->seed = 0;
+    return NC_OK;
+}
+
+int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int32_t* syn_from,
+              const int32_t* syn_to, const float* syn_weight, const float* syn_length,
+              const uint8_t* syn_inhibitory, const nc_params* params, nc_net** out)
+{
+    if (!out || !params) return fail(NC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
+        return fail(NC_ERR_NODEVICE, "no CUDA device: the GB300 step has no CPU fallback");
+    nc_net* net = new (std::nothrow) nc_net();
+    if (!net) return fail(NC_ERR_NOMEM, "host allocation failed");
+    std::string err;
+    int rc = nc::build_net(n_neurons, xyz, n_synapses, syn_from, syn_to, syn_weight, syn_length, syn_inhibitory,
+                           *params, net->host, err);
+    if (rc == NC_OK) {
+        std::vector<const nc::NetHost*> nets{&net->host};
+        rc = net->eng.build(nets, 64, err);
+    }
+    if (rc != NC_OK) {
+        delete net;
+        return fail(rc, err);
+    }
+    // keep on the host only what read-back needs
+    nc::NetHost& h = net->host;
+    std::vector<int32_t>().swap(h.out_post);
+    std::vector<int32_t>().swap(h.out_csc);
+    std::vector<int16_t>().swap(h.out_delay);
+    std::vector<uint32_t>().swap(h.out_ringpos);
+    std::vector<float>().swap(h.w);
+    std::vector<int64_t>().swap(h.in_ptr);
+    std::vector<int32_t>().swap(h.ring_off);
+    *out = net;
+    return NC_OK;
+}
+
+int nc_destroy(nc_net* net)
+{
+    if (!net) return NC_OK;
+    cudaSetDevice(net->eng.device);
+    delete net;
+    return NC_OK;
+}
+
+int nc_set_input_groups(nc_net* net, int32_t n_groups, const nc_group* groups)
+{
+    NC_NEED(net);
+    std::string err;
+    int rc = nc::set_groups(net->host, n_groups, groups, err);
+    if (rc != NC_OK) return fail(rc, err);
+    NC_CALL(net->eng, set_groups, 0, net->host.groups);
+    return NC_OK;
+}
+
+int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
+                            const float* radius)
+{
+    (void)rates_hz; (void)count; (void)xyz; (void)radius;
+    if (!net) return fail(NC_ERR_INVALID, "null handle");
+    return fail(NC_ERR_UNSUPPORTED, "periodic input firers are not implemented in the stepped GPU model; "
+                                    "use nc_set_input_groups or nc_schedule_fire");
+}
+
+int nc_set_rates(nc_net* net, float learning_rate, float presynaptic_factor, float postsynaptic_factor)
+{
+    NC_NEED(net);
+    NC_CALL(net->eng, set_rates, 0, learning_rate, presynaptic_factor, postsynaptic_factor);
+    net->host.p.learning_rate = learning_rate;
+    net->host.p.presynaptic_factor = presynaptic_factor;
+    net->host.p.postsynaptic_factor = postsynaptic_factor;
+    return NC_OK;
+}
+
+int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* ids)
+{
+    NC_NEED(net);
+    if (count < 0 || (count > 0 && !ids)) return fail(NC_ERR_INVALID, "bad id array");
+    for (int32_t k = 0; k < count; ++k)
+        if (ids[k] < 0 || ids[k] >= net->host.n) return fail(NC_ERR_INVALID, "neuron id out of range");
+    NC_CALL(net->eng, force_fire, 0, ids, count);
+    return NC_OK;
+}
+
+int nc_run(nc_net* net, int32_t n_steps)
+{
+    NC_NEED(net);
+    if (n_steps < 0) return fail(NC_ERR_INVALID, "negative step count");
+    if (net->step + n_steps >= (1ll << 30)) return fail(NC_ERR_INVALID, "step counter limit reached");
+    NC_CALL(net->eng, step, (int64_t)n_steps);
+    net->step += n_steps;
+    for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;  // currentTime = targetTime
+    return NC_OK;
+}
+
+int nc_sync(nc_net* net)
+{
+    NC_NEED(net);
+    NC_CALL0(net->eng, sync);
+    return NC_OK;
+}
+
+int nc_get_time(nc_net* net, float* ms)
+{
+    if (!net || !ms) return fail(NC_ERR_INVALID, "null argument");
+    *ms = net->time;
+    return NC_OK;
+}
+
+int nc_get_step(nc_net* net, int64_t* step)
+{
+    if (!net || !step) return fail(NC_ERR_INVALID, "null argument");
+    *step = net->step;
+    return NC_OK;
+}
+
+int nc_get_counts(nc_net* net, int32_t* n_neurons, int64_t* n_synapses)
+{
+    if (!net) return fail(NC_ERR_INVALID, "null handle");
+    if (n_neurons) *n_neurons = net->host.n;
+    if (n_synapses) *n_synapses = net->host.s;
+    return NC_OK;
+}
+
+int nc_record_raster(nc_net* net, int32_t max_steps)
+{
+    NC_NEED(net);
+    if (max_steps < 0) return fail(NC_ERR_INVALID, "negative step count");
+    NC_CALL0(net->eng, sync);
+    net->raster_t0 = (int32_t)net->step + 1;
+    if (net->d_raster && max_steps != net->raster_cap) {
+        cudaFree(net->d_raster);
+        net->d_raster = nullptr;
+        net->raster_cap = 0;
+    }
+    if (max_steps > 0 && !net->d_raster) {
+        const size_t words = (size_t)max_steps * net->eng.slots[0].n_words;
+        cudaError_t e = cudaMalloc(&net->d_raster, std::max<size_t>(words, 1) * sizeof(uint32_t));
+        if (e != cudaSuccess) return fail(NC_ERR_NOMEM, nc::cuda_msg("cudaMalloc raster", e));
+        e = cudaMemset(net->d_raster, 0, std::max<size_t>(words, 1) * sizeof(uint32_t));
+        if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("cudaMemset raster", e));
+        net->raster_cap = max_steps;
+    }
+    NC_CALL(net->eng, set_raster, 0, net->d_raster, net->raster_t0, net->raster_cap);
+    return NC_OK;
+}
+
+int nc_read_raster(nc_net* net, uint8_t* out, int64_t capacity_bytes, int32_t* steps)
+{
+    NC_NEED(net);
+    if (!steps) return fail(NC_ERR_INVALID, "null steps");
+    const int64_t done = net->step - net->raster_t0 + 1;
+    const int32_t rows = (int32_t)std::max<int64_t>(0, std::min<int64_t>(done, net->raster_cap));
+    const int32_t nw = net->eng.slots[0].n_words;
+    const int64_t row_bytes = ((int64_t)net->host.n + 7) / 8;
+    *steps = rows;
+    if (!out) return NC_OK;
+    if (capacity_bytes < rows * row_bytes) return fail(NC_ERR_INVALID, "raster buffer too small");
+    std::vector<uint32_t> buf((size_t)rows * nw);
+    NC_CALL(net->eng, download, buf.data(), (const uint32_t*)net->d_raster, buf.size());
+    for (int32_t r = 0; r < rows; ++r)
+        std::memcpy(out + (int64_t)r * row_bytes, buf.data() + (size_t)r * nw, (size_t)row_bytes);
+    return NC_OK;
+}
+
+int nc_read_potentials(nc_net* net, float* out_n)
+{
+    NC_NEED(net);
+    if (!out_n && net->host.n) return fail(NC_ERR_INVALID, "null output");
+    const auto& sl = net->eng.slots[0];
+    NC_CALL(net->eng, download, out_n, (const float*)net->eng.P.pot + sl.neuron_base, (size_t)sl.n);
+    return NC_OK;
+}
+
+int nc_read_potact(nc_net* net, float* out_2n)
+{
+    NC_NEED(net);
+    const int32_t n = net->host.n;
+    if (!out_2n && n) return fail(NC_ERR_INVALID, "null output");
+    std::vector<float> pot((size_t)n);
+    std::vector<uint32_t> fir((size_t)n);
+    std::vector<int32_t> start((size_t)n);
+    const auto& sl = net->eng.slots[0];
+    NC_CALL(net->eng, download, pot.data(), (const float*)net->eng.P.pot + sl.neuron_base, (size_t)n);
+    NC_CALL(net->eng, download, fir.data(), (const uint32_t*)net->eng.P.firings + sl.neuron_base, (size_t)n);
+    NC_CALL(net->eng, download, start.data(), (const int32_t*)net->eng.P.act_start + sl.neuron_base, (size_t)n);
+    const float dt = net->host.dt;
+    const int64_t t = net->step;
+    for (int32_t j = 0; j < n; ++j) {
+        out_2n[2 * (size_t)j] = pot[j];
+        // setActivity(firings/(((float) currentT-activityStartTime)/10.0)) at the last update
+        float act = 0.0f;
+        if (t >= 1 && t > start[j])
+            act = (float)(fir[j] / (((float)nc::step_ms(t, dt) - nc::step_ms(start[j], dt)) / 10.0));
+        out_2n[2 * (size_t)j + 1] = act;
+    }
+    return NC_OK;
+}
+
+int nc_read_positions(nc_net* net, float* out_3n)
+{
+    if (!net || (!out_3n && net->host.n)) return fail(NC_ERR_INVALID, "null argument");
+    std::memcpy(out_3n, net->host.xyz.data(), sizeof(float) * net->host.xyz.size());
+    return NC_OK;
+}
+
+int nc_read_last_fire(nc_net* net, float* out_n)
+{
+    NC_NEED(net);
+    const int32_t n = net->host.n;
+    if (!out_n && n) return fail(NC_ERR_INVALID, "null output");
+    std::vector<int32_t> lf((size_t)n);
+    NC_CALL(net->eng, download, lf.data(), (const int32_t*)net->eng.P.lf + net->eng.slots[0].neuron_base, (size_t)n);
+    for (int32_t j = 0; j < n; ++j) out_n[j] = lf[j] == NC_NEVER ? NAN : nc::step_ms(lf[j], net->host.dt);
+    return NC_OK;
+}
+
+int nc_read_weights(nc_net* net, float* out_s)
+{
+    NC_NEED(net);
+    const nc::NetHost& h = net->host;
+    if (!out_s && h.n_input) return fail(NC_ERR_INVALID, "null output");
+    NC_CALL0(net->eng, flush_plasticity);
+    std::vector<float> w((size_t)h.s);
+    NC_CALL(net->eng, download, w.data(), (const float*)net->eng.P.w + net->eng.slots[0].syn_base, (size_t)h.s);
+    for (int64_t k = 0; k < h.n_input; ++k) {
+        const int64_t c = h.input_to_csc[(size_t)k];
+        out_s[k] = c < 0 ? NAN : w[(size_t)c];
+    }
+    return NC_OK;
+}
+
+int nc_read_delays(nc_net* net, int32_t* out_s)
+{
+    if (!net || (!out_s && net->host.n_input)) return fail(NC_ERR_INVALID, "null argument");
+    const nc::NetHost& h = net->host;
+    for (int64_t k = 0; k < h.n_input; ++k) {
+        const int64_t c = h.input_to_csc[(size_t)k];
+        out_s[k] = c < 0 ? -1 : h.csc_delay[(size_t)c];
+    }
+    return NC_OK;
+}
+
+int nc_read_inhibitory(nc_net* net, uint8_t* out_s)
+{
+    if (!net || (!out_s && net->host.n_input)) return fail(NC_ERR_INVALID, "null argument");
+    const nc::NetHost& h = net->host;
+    for (int64_t k = 0; k < h.n_input; ++k) {
+        const int64_t c = h.input_to_csc[(size_t)k];
+        out_s[k] = c < 0 ? 255 : (nc::inhibitory_flag(h, c) ? 1 : 0);
+    }
+    return NC_OK;
+}
+
+int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t capacity, int64_t* count)
+{
+    NC_NEED(net);
+    if (!count) return fail(NC_ERR_INVALID, "null count");
+    const nc::NetHost& h = net->host;
+    *count = h.s;
+    if (!out) return NC_OK;
+    if (capacity < h.s) return fail(NC_ERR_INVALID, "snapshot buffer too small");
+    NC_CALL0(net->eng, flush_plasticity);
+    const auto& sl = net->eng.slots[0];
+    const auto& P = net->eng.P;
+    std::vector<float> w((size_t)h.s);
+    std::vector<int32_t> post((size_t)h.s), csc((size_t)h.s), la((size_t)h.s);
+    std::vector<int16_t> dly((size_t)h.s);
+    std::vector<int64_t> optr((size_t)h.n + 1);
+    NC_CALL(net->eng, download, w.data(), (const float*)P.w + sl.syn_base, (size_t)h.s);
+    NC_CALL(net->eng, download, post.data(), (const int32_t*)P.out_post + sl.syn_base, (size_t)h.s);
+    NC_CALL(net->eng, download, csc.data(), (const int32_t*)P.out_csc + sl.syn_base, (size_t)h.s);
+    NC_CALL(net->eng, download, la.data(), (const int32_t*)P.last_arr + sl.syn_base, (size_t)h.s);
+    NC_CALL(net->eng, download, dly.data(), (const int16_t*)P.out_delay + sl.syn_base, (size_t)h.s);
+    NC_CALL(net->eng, download, optr.data(), (const int64_t*)P.out_ptr + sl.ptr_base, (size_t)h.n + 1);
+    const float T = net->time;
+    const int64_t t = net->step;
+    for (int32_t i = 0; i < h.n; ++i) {
+        for (int64_t k = optr[i] - sl.syn_base; k < optr[i + 1] - sl.syn_base; ++k) {
+            nc_synapse_snapshot& o = out[k];
+            const float weight = w[(size_t)csc[(size_t)k]];
+            o.from_id = i;
+            o.to_id = post[(size_t)k];
+            o.weight = weight;
+            o.inhibitory = weight < 0.0f;
+            o.pre_potential = 0.0f;
+            o.post_potential = 0.0f;
+            const int32_t a = la[(size_t)k];
+            // in flight (AP_fireTime != 0) until its target's update KC steps after arrival
+            if (a == NC_NEVER || t - a >= h.kc) continue;
+            const int32_t d = dly[(size_t)k];
+            const float length_speed = ((float)d * h.dt / 2.0f) * 2.0f;  // length*AP_speed
+            const float fire_time = nc::step_ms(a, h.dt);                  // AP_fireTime
+            const float start = nc::step_ms(a - d, h.dt);                  // lastSpikeStart
+            o.pre_potential = render_behaviour((float)(T - start) / length_speed) * weight;
+            if (T < fire_time) o.post_potential = render_behaviour((float)(fire_time - T) / length_speed) * weight;
+        }
+    }
+    return NC_OK;
+}
+
+int nc_reset_activities(nc_net* net)
+{
+    NC_NEED(net);
+    const auto& sl = net->eng.slots[0];
+    std::vector<int32_t> start((size_t)sl.n, (int32_t)net->step);
+    cudaError_t e = cudaMemcpyAsync(net->eng.P.act_start + sl.neuron_base, start.data(), sizeof(int32_t) * sl.n,
+                                    cudaMemcpyHostToDevice, net->eng.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(net->eng.P.firings + sl.neuron_base, 0, sizeof(uint32_t) * sl.n,
+                                              net->eng.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(net->eng.stream);
+    if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("reset activities", e));
+    return NC_OK;
+}
+
+int nc_get_stats(nc_net* net, nc_stats* out)
+{
+    NC_NEED(net);
+    if (!out) return fail(NC_ERR_INVALID, "null output");
+    unsigned long long s[4];
+    NC_CALL(net->eng, read_stats, 0, s);
+    out->fires = (int64_t)s[0];
+    out->launched = (int64_t)s[1];
+    out->dropped = (int64_t)s[2];
+    out->steps = (int64_t)s[3];
+    return NC_OK;
+}
+
+int nc_delete_synapse(nc_net* net, int32_t from_id, int32_t to_id)
+{
+    (void)net; (void)from_id; (void)to_id;
+    return fail(NC_ERR_UNSUPPORTED, "topology mutation is outside the GPU step model");
+}
+
+int nc_delete_neuron(nc_net* net, int32_t id)
+{
+    (void)net; (void)id;
+    return fail(NC_ERR_UNSUPPORTED, "topology mutation is outside the GPU step model");
+}
+
+int nc_time_steps(nc_net* net, int32_t n_steps, float* ms, float* kernel_ms)
+{
+    NC_NEED(net);
+    if (n_steps < 0 || !ms) return fail(NC_ERR_INVALID, "bad argument");
+    NC_CALL(net->eng, step_timed, (int64_t)n_steps, ms);
+    net->step += n_steps;
+    for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;
+    if (kernel_ms) {
+        const int m = std::min(n_steps, 200);
+        NC_CALL(net->eng, time_kernels, m, &kernel_ms[0], &kernel_ms[1]);
+        net->step += m;
+        for (int k = 0; k < m; ++k) net->time = net->time + net->host.dt;
+    }
+    return NC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+// nc_engine.cuh — data layout shared by the step kernels and the host engine.
+//
+// One engine advances one or more independent networks ("nets") packed into
+// pooled device arrays.  A single network (nc_create) is an engine with one net;
+// the batched and served forms pack many.  Every net keeps its own step counter,
+// constants, input groups and draw key, and no array is shared between nets, so a
+// net computes the same bits alone or packed with others.
+//
+// Per net, in HBM:
+//   neurons   pot, lf (last fire step), firings, act_start     SoA, pool-indexed
+//   in_ptr    CSC row starts (n+1): in-synapses of target j, ascending source id
+//             — the order of the reference's std::map inSynapses (src/NeuCor.h:212)
+//   w, t_arr, term          per in-synapse (CSC order): weight, last arrival step,
+//                           contribution term captured at launch (double)
+//   inh                     one bit per in-synapse: Synapse::inhibitory
+//   out_ptr   CSR row starts (n+1) and per out-synapse (CSR order): target,
+//             CSC index, delay, ring bit position, last accepted arrival step
+//   ring      R slots x W words: bit b of target j's words in slot a mod R set when
+//             the spike on j's b-th in-synapse arrives at step a
+//   fired / forced   two parities of one bit per neuron
+#pragma once
+#include <cstdint>
+#include <vector_types.h>
+
+#ifdef __CUDACC__
+#define NC_HD __host__ __device__
+#else
+#define NC_HD
+#endif
+
+#define NC_NEVER INT32_MIN
+
+// Draw streams (third Philox counter word).
+#define NC_STREAM_BACKGROUND 1u
+#define NC_STREAM_SOURCE 2u
+#define NC_STREAM_JITTER 3u
+#define NC_STREAM_INDEPENDENT 4u
+
+struct NcGroupDev {
+    int32_t first;
+    int32_t count;
+    uint32_t thresh;     // Bernoulli threshold of the per-step probability, on a 32-bit draw
+    int32_t correlated;
+    int32_t jitter;
+    int32_t index;       // group index within its net (first Philox counter word)
+};
+
+struct NcNetDesc {
+    int32_t t;            // step processed by the next launch pair (>= 1)
+    int32_t t_end;        // last step to simulate (inclusive)
+    int32_t stdp_done;    // last step whose deferred plasticity has been applied
+    int32_t n;            // neurons
+    int32_t neuron_base;  // pool index of neuron 0
+    int32_t ptr_base;     // pool index of in_ptr/out_ptr/ring_off entry 0 (n+1 entries)
+    int32_t word_base;    // pool index of this net's first bitset word
+    int32_t n_words;      // ceil(n/32)
+    int64_t syn_base;     // pool index of synapse 0 (CSC and CSR arrays)
+    int64_t ring_base;    // pool word index of ring slot 0
+    int32_t ring_words;   // words per slot
+    int32_t ring_mask;    // slots - 1
+    int32_t kc;           // smallest k >= 1 with 2.0f < k*dt (AP_cutoff, src/NeuCor.cpp:385)
+    int32_t bg_period;    // max(1, int(600/dt)); 0 = background off
+    uint32_t key0, key1;  // Philox key
+    int32_t table_base;   // pool index of the trace tables
+    int32_t tab_pre_len;  // presynaptic trace table length
+    int32_t tab_post_len; // postsynaptic trace table length
+    int32_t ap_base;      // pool index of the AP shape table (kc entries)
+    int32_t group_base;
+    int32_t n_groups;
+    int32_t active;       // 0: skipped by the kernels
+    int32_t raster_len;   // recorded steps capacity (0 = off)
+    int32_t raster_t0;    // first recorded step
+    int32_t pad0;
+    float dt;
+    float leak;           // powf(0.5f, dt)  (src/NeuCor.cpp:678)
+    float c52;            // float(0.2f * 52.0) (src/NeuCor.cpp:729-730)
+    float lr, pre_factor, post_factor;
+    double e_term;        // 0.9943 is applied separately; this is exp(0.3702*dt) (src/NeuCor.cpp:695)
+    uint32_t* raster;     // device raster rows of n_words words
+    unsigned long long* stats; // 4 counters: fires, launched, dropped, steps
+};
+
+struct NcTile {          // 32 consecutive neurons of one net
+    int32_t net;
+    int32_t first;       // local id of the first neuron (multiple of 32)
+};
+
+struct NcPools {
+    // neurons
+    float* pot;
+    int32_t* lf;
+    uint32_t* firings;
+    int32_t* act_start;
+    // per-neuron pointers (n+1 per net)
+    int64_t* in_ptr;     // absolute CSC index
+    int64_t* out_ptr;    // absolute CSR index
+    int32_t* ring_off;   // word offset within a slot
+    // in-synapses (CSC); every net's synapse base is a multiple of 32
+    float* w;
+    uint32_t* inh;       // Synapse::inhibitory, one bit per synapse
+    int32_t* t_arr;
+    double* term;
+    // out-synapses (CSR)
+    int32_t* out_post;   // local target id
+    int32_t* out_csc;    // CSC index relative to syn_base
+    int16_t* out_delay;
+    uint32_t* out_ringpos; // (word within slot) << 5 | bit
+    int32_t* last_arr;
+    // ring and bitsets
+    uint32_t* ring;
+    uint32_t* fired;     // 2 parities x total_words
+    uint32_t* forced;    // 2 parities x total_words
+    int64_t total_words;
+    // fired list (global, 2 parities)
+    int2* fired_list;    // (net, local id)
+    int32_t* fired_count;// [2]
+    int64_t fired_cap;
+    // constants
+    float* tables;
+    NcGroupDev* groups;
+    NcNetDesc* nets;
+    int32_t n_nets;
+    NcTile* tiles;
+    int32_t n_tiles;
+    // engine
+    int32_t* tick;       // engine tick (parity of the fired list)
+    uint32_t* done_ctr;  // last-block detection
+};
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+NC_HD inline void nc_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                          uint32_t k1, uint32_t out[4])
+{
+#ifdef __CUDACC__
+#pragma unroll
+#endif
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+#ifdef __CUDA_ARCH__
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+// Kernel launchers (nc_kernels.cu).
+namespace nc {
+struct LaunchShape {
+    int neuron_block;    // threads per block of the neuron-update kernel (multiple of 32)
+    int launch_blocks;   // blocks of the spike-launch kernel
+    int launch_block;    // threads per block of the spike-launch kernel
+};
+int launch_neuron_step(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_spike_launch(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_stdp_flush(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
+int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);
+}  // namespace nc

@@ -132,7 +132,18 @@ void ncs_default_params(ncs_params* p)
     p->presynaptic_factor = 0.13f;
     p->postsynaptic_factor = 0.30f;
     p->background_firing = 1;
+    p->inhibitory_rule = NCS_INHIBITORY_COPY_LOSS;
     p->seed = 0;
+}
+
+/* Whether the m-th synapse (0-based) appended to an outSynapses vector of final size
+ * `size` was copied by a reallocation: the vector is reserved to 5 (NeuCor.cpp:374)
+ * and libstdc++ doubles its capacity when full. */
+static int grown_copy(int64_t m, int64_t size)
+{
+    int64_t cap = 5;
+    while (cap <= m) cap *= 2;
+    return size > cap;
 }
 
 static float kdt(const ncs_net* h, int32_t k) { return (float)k * h->dt; }
@@ -181,7 +192,7 @@ static int cmp_key3(const void* a, const void* b)
 
 ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* syn_pre,
                     const int32_t* syn_post, const float* syn_weight, const float* syn_length,
-                    const ncs_params* params)
+                    const uint8_t* syn_inhibitory, const ncs_params* params)
 {
     if (n < 0 || n_syn < 0 || !params) return NULL;
     if (!(params->run_speed > 0.0f)) return NULL;
@@ -236,7 +247,7 @@ ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* s
         h->post_ptr[keys[c].post + 1]++;
         /* Synapse ctor + setWeight: weight, inhibitory = weight < 0 (NeuCor.cpp:475,576-579) */
         h->w[c] = syn_weight[k];
-        h->inh[c] = syn_weight[k] < 0.0f;
+        h->inh[c] = syn_weight[k] < 0.0f;  /* replaced below for copied synapses */
         float len = syn_length ? syn_length[k]
                                : get_dist(&xyz[3 * (int64_t)keys[c].pre], &xyz[3 * (int64_t)keys[c].post]);
         int32_t d = delay_steps(len, h->dt);
@@ -251,17 +262,31 @@ ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* s
     for (int32_t j = 0; j < n; ++j) h->post_ptr[j + 1] += h->post_ptr[j];
     free(keys);
 
+    /* out-synapses of each source in creation order (Neuron::outSynapses) */
     h->out_ptr = (int64_t*)xcalloc((size_t)n + 1, sizeof(int64_t));
     h->out_syn = (int64_t*)xcalloc((size_t)s, sizeof(int64_t));
     for (int64_t c = 0; c < s; ++c) h->out_ptr[h->pre[c] + 1]++;
     for (int32_t j = 0; j < n; ++j) h->out_ptr[j + 1] += h->out_ptr[j];
     {
         int64_t* fill = (int64_t*)xcalloc((size_t)n + 1, sizeof(int64_t));
-        for (int64_t c = 0; c < s; ++c) {
+        for (int64_t k = 0; k < n_syn; ++k) {
+            int64_t c = h->input_to_csc[k];
+            if (c < 0) continue;
             int32_t i = h->pre[c];
             h->out_syn[h->out_ptr[i] + fill[i]++] = c;
         }
         free(fill);
+    }
+    if (params->inhibitory_rule == NCS_INHIBITORY_COPY_LOSS) {
+        for (int32_t i = 0; i < n; ++i) {
+            int64_t size = h->out_ptr[i + 1] - h->out_ptr[i];
+            for (int64_t m = 0; m < size; ++m)
+                if (grown_copy(m, size)) h->inh[h->out_syn[h->out_ptr[i] + m]] = 0;
+        }
+    }
+    if (syn_inhibitory) {
+        for (int64_t k = 0; k < n_syn; ++k)
+            if (h->input_to_csc[k] >= 0) h->inh[h->input_to_csc[k]] = syn_inhibitory[k] ? 1 : 0;
     }
 
     /* Neuron ctor, NeuCor.cpp:368-395 */
@@ -587,6 +612,11 @@ void ncs_read_last_fire_step(const ncs_net* h, int32_t* out) { memcpy(out, h->lf
 void ncs_read_weights(const ncs_net* h, float* out)
 {
     for (int64_t k = 0; k < h->n_input; ++k) out[k] = h->input_to_csc[k] < 0 ? NAN : h->w[h->input_to_csc[k]];
+}
+
+void ncs_read_inhibitory(const ncs_net* h, uint8_t* out)
+{
+    for (int64_t k = 0; k < h->n_input; ++k) out[k] = h->input_to_csc[k] < 0 ? 255 : h->inh[h->input_to_csc[k]];
 }
 
 void ncs_read_delays(const ncs_net* h, int32_t* out)

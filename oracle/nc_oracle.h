@@ -38,9 +38,20 @@ typedef struct {
     float presynaptic_factor;       /* NeuCor.h:73 */
     float postsynaptic_factor;
     int32_t background_firing;      /* 1: NeuCor.cpp:604-607 background fires; 0: off */
-    int32_t reserved;
+    int32_t inhibitory_rule;        /* NCS_INHIBITORY_* (see below) */
     uint64_t seed;                  /* Philox key for background and input draws */
 } ncs_params;
+
+/* Synapse::inhibitory (NeuCor.h:290) is set from the weight's sign by setWeight
+ * (NeuCor.cpp:576-579), but the Synapse copy constructor (NeuCor.cpp:487-504) does not
+ * copy it: a synapse copied when its source's outSynapses vector grows (reserve(5),
+ * NeuCor.cpp:374, then capacity doubling) reads an indeterminate flag.
+ *   NCS_INHIBITORY_COPY_LOSS: copied synapses are not inhibitory (the value the
+ *     reference shows when the grown vector lands in fresh memory);
+ *   NCS_INHIBITORY_SIGN: inhibitory = weight < 0 for every synapse.
+ * Explicit per-synapse flags passed to ncs_create override the rule. */
+#define NCS_INHIBITORY_COPY_LOSS 0
+#define NCS_INHIBITORY_SIGN 1
 
 typedef struct {
     int32_t first;        /* first neuron id of the group */
@@ -65,11 +76,14 @@ void ncs_default_params(ncs_params* p);
 /* Builds a network from explicit neurons and synapses (NeuCor::createNeuron /
  * createSynapse, NeuCor.cpp:154-195).  syn_length may be NULL: lengths are then
  * coord3::getDist of the endpoints (NeuCor.h:16-18, NeuCor.cpp:477-479).
+ * syn_inhibitory may be NULL: flags then follow params->inhibitory_rule.
  * Returns NULL on bad input. */
 ncs_net* ncs_create(int32_t n_neurons, const float* xyz, int64_t n_syn,
                     const int32_t* syn_pre, const int32_t* syn_post,
                     const float* syn_weight, const float* syn_length,
-                    const ncs_params* params);
+                    const uint8_t* syn_inhibitory, const ncs_params* params);
+/* Effective inhibitory flag of every input synapse (0/1; 255 for duplicates). */
+void ncs_read_inhibitory(const ncs_net* h, uint8_t* out);
 void ncs_destroy(ncs_net* h);
 
 int ncs_set_groups(ncs_net* h, int32_t n_groups, const ncs_group* groups);

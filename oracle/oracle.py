@@ -32,9 +32,13 @@ class Params(ctypes.Structure):
         ("presynaptic_factor", ctypes.c_float),
         ("postsynaptic_factor", ctypes.c_float),
         ("background_firing", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("inhibitory_rule", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
     ]
+
+
+INHIBITORY_COPY_LOSS = 0
+INHIBITORY_SIGN = 1
 
 
 class Group(ctypes.Structure):
@@ -78,7 +82,8 @@ def lib() -> ctypes.CDLL:
         L = ctypes.CDLL(LIB_PATH)
         P = ctypes.c_void_p
         L.ncs_create.restype = P
-        L.ncs_create.argtypes = [ctypes.c_int32, P, ctypes.c_int64, P, P, P, P, ctypes.POINTER(Params)]
+        L.ncs_create.argtypes = [ctypes.c_int32, P, ctypes.c_int64, P, P, P, P, P, ctypes.POINTER(Params)]
+        L.ncs_read_inhibitory.argtypes = [P, P]
         L.ncs_destroy.argtypes = [P]
         L.ncs_set_groups.argtypes = [P, ctypes.c_int32, P]
         L.ncs_set_rates.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float]
@@ -136,7 +141,8 @@ def philox(ctr, key):
 class OracleS:
     """The stepped CPU restatement of NeuCor::run (runAll=true, fixed dt)."""
 
-    def __init__(self, xyz, pre, post, weight, length=None, params: Params | None = None, groups=()):
+    def __init__(self, xyz, pre, post, weight, length=None, params: Params | None = None, groups=(),
+                 inhibitory=None):
         self.xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
         self.n = int(self.xyz.shape[0])
         self.pre = np.ascontiguousarray(pre, dtype=np.int32)
@@ -145,8 +151,9 @@ class OracleS:
         self.length = None if length is None else np.ascontiguousarray(length, dtype=np.float32)
         self.params = params if params is not None else default_params()
         self.n_input = int(self.pre.shape[0])
+        self.inh_in = None if inhibitory is None else np.ascontiguousarray(inhibitory, dtype=np.uint8)
         self.h = lib().ncs_create(self.n, _ptr(self.xyz), self.n_input, _ptr(self.pre), _ptr(self.post),
-                                  _ptr(self.weight), _ptr(self.length), ctypes.byref(self.params))
+                                  _ptr(self.weight), _ptr(self.length), _ptr(self.inh_in), ctypes.byref(self.params))
         if not self.h:
             raise ValueError("oracle rejected the network")
         if groups:
@@ -200,6 +207,11 @@ class OracleS:
         lib().ncs_read_weights(self.h, _ptr(o))
         return o
 
+    def inhibitory(self):
+        o = np.zeros(self.n_input, dtype=np.uint8)
+        lib().ncs_read_inhibitory(self.h, _ptr(o))
+        return o
+
     def delays(self):
         o = np.zeros(self.n_input, dtype=np.int32)
         lib().ncs_read_delays(self.h, _ptr(o))
@@ -230,7 +242,7 @@ def background_draws(seed: int, n: int, dt: float, counter: int):
 
 
 # ------------------------------------------------------------- Oracle-R runner
-MODES = {"canonical": 0, "native": 1, "continuous": 2}
+MODES = {"canonical": 0, "native": 1, "continuous": 2, "construct": 4}
 
 
 def reference_available() -> bool:
@@ -293,8 +305,46 @@ def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps
     ckw = np.frombuffer(data, dtype=np.float32, count=s * len(checkpoints), offset=off).reshape(len(checkpoints), s)
     off += 4 * s * len(checkpoints)
     fin = np.frombuffer(data, dtype=np.float32, count=3 * n, offset=off)
+    off += 12 * n
+    inh = np.frombuffer(data, dtype=np.uint8, count=s, offset=off)
     return {"raster": raster.copy(), "pots": None if pots is None else pots.copy(), "weights": ckw.copy(),
-            "pot": fin[:n].copy(), "activity": fin[n:2 * n].copy(), "last_fire": fin[2 * n:].copy()}
+            "pot": fin[:n].copy(), "activity": fin[n:2 * n].copy(), "last_fire": fin[2 * n:].copy(),
+            "inhibitory": inh.copy()}
+
+
+def reference_construct(n: int, seed: int):
+    """srand(seed); NeuCor(n) in the reference: positions and synapses (from, to,
+    weight, length) in the reference's own order."""
+    p = default_params(seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        scen = os.path.join(td, "s.bin")
+        outp = os.path.join(td, "o.bin")
+        with open(scen, "wb") as f:
+            f.write(b"NCRF")
+            f.write(struct.pack("<iiq", MODES["construct"], n, 0))
+            f.write(np.zeros(3 * n, np.float32).tobytes())
+            f.write(struct.pack("<6f", p.run_speed, p.learning_rate, p.presynaptic_trace_decay,
+                                p.postsynaptic_trace_decay, p.presynaptic_factor, p.postsynaptic_factor))
+            f.write(struct.pack("<iQ", p.background_firing, p.seed))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<ii", 0, 0))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", 0))
+        subprocess.run([REF_BIN, scen, outp], check=True)
+        data = open(outp, "rb").read()
+    s = struct.unpack_from("<q", data, 0)[0]
+    off = 8
+    xyz = np.frombuffer(data, np.float32, 3 * n, off).reshape(n, 3).copy()
+    off += 12 * n
+    fr = np.frombuffer(data, np.int32, s, off).copy()
+    off += 4 * s
+    to = np.frombuffer(data, np.int32, s, off).copy()
+    off += 4 * s
+    w = np.frombuffer(data, np.float32, s, off).copy()
+    off += 4 * s
+    ln = np.frombuffer(data, np.float32, s, off).copy()
+    return xyz, fr, to, w, ln
 
 
 def unpack_raster(raster, n):

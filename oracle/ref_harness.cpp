@@ -23,6 +23,9 @@
 //                  at the new T so each step ends with all neurons updated.
 //   2 continuous — NeuCor::run alone, synapse lengths as constructed (spikes
 //                  arrive between steps), background firing from glibc rand().
+//   4 construct  — srand(seed); NeuCor(n) (NeuCor.cpp:17-42); writes the positions
+//                  and every synapse (source, target, weight, length) in the
+//                  reference's own order.
 // Modes 0 and 1 set every synapse length to delay*dt/AP_speed so spikes arrive
 // on the step grid.
 #include "NeuCor.h"
@@ -122,6 +125,11 @@ static Scenario read_scenario(const char* path)
 }
 
 // ------------------------------------------------------------------ driver
+class NeuCor_Renderer;
+struct NeuCor_Lengths {
+    static void collect(NeuCor& brain, std::vector<float>& out);
+};
+
 class NeuCor_Renderer {
 public:
     explicit NeuCor_Renderer(const Scenario& sc) : sc_(sc) {}
@@ -232,6 +240,14 @@ public:
             fin[2 * n + j] = brain_->neurons[j].lastFire;
         }
         fwrite(fin.data(), sizeof(float), fin.size(), out);
+        // the reference's own Synapse::inhibitory flags (never changed after construction)
+        std::vector<uint8_t> inh(sc_.s, 255);
+        for (int64_t k = 0; k < sc_.s; ++k) {
+            if (!first_[k]) continue;
+            const Synapse* syn = brain_->getSynapse((std::size_t)sc_.pre[k], (std::size_t)sc_.post[k]);
+            inh[k] = syn && syn->inhibitory ? 1 : 0;
+        }
+        fwrite(inh.data(), 1, inh.size(), out);
         fclose(out);
         delete brain_;
         return 0;
@@ -270,11 +286,43 @@ private:
         }
     }
 
+    friend struct NeuCor_Lengths;
+    static void lengths(NeuCor& brain, std::vector<float>& out)
+    {
+        for (auto& neu : brain.neurons)
+            for (auto& syn : neu.outSynapses) out.push_back(syn.length);
+    }
+
     const Scenario& sc_;
     NeuCor* brain_ = nullptr;
     std::vector<uint8_t> first_;
     std::vector<float> rates_;
 };
+
+void NeuCor_Lengths::collect(NeuCor& brain, std::vector<float>& out) { NeuCor_Renderer::lengths(brain, out); }
+
+static int construct(const Scenario& sc, const char* out_path)
+{
+    srand((unsigned)sc.p.seed);
+    NeuCor brain(sc.n);
+    FILE* out = fopen(out_path, "wb");
+    if (!out) { perror(out_path); return 2; }
+    std::vector<float> xyz;
+    std::vector<int32_t> from, to;
+    std::vector<float> w, len;
+    for (const auto& p : brain.getNeuronSnapshots()) { xyz.push_back(p.position.x); xyz.push_back(p.position.y); xyz.push_back(p.position.z); }
+    for (const auto& s : brain.getSynapseSnapshots()) { from.push_back((int32_t)s.fromID); to.push_back((int32_t)s.toID); w.push_back(s.weight); }
+    NeuCor_Lengths::collect(brain, len);
+    int64_t ns = (int64_t)from.size();
+    fwrite(&ns, sizeof(ns), 1, out);
+    fwrite(xyz.data(), sizeof(float), xyz.size(), out);
+    fwrite(from.data(), sizeof(int32_t), from.size(), out);
+    fwrite(to.data(), sizeof(int32_t), to.size(), out);
+    fwrite(w.data(), sizeof(float), w.size(), out);
+    fwrite(len.data(), sizeof(float), len.size(), out);
+    fclose(out);
+    return 0;
+}
 
 int main(int argc, char** argv)
 {
@@ -283,6 +331,7 @@ int main(int argc, char** argv)
         return 2;
     }
     Scenario sc = read_scenario(argv[1]);
+    if (sc.mode == 4) return construct(sc, argv[2]);
     srand((unsigned)sc.p.seed);
     NeuCor_Renderer drv(sc);
     return drv.run(argv[2]);

@@ -1,0 +1,97 @@
+"""Generates the golden fixtures in this directory from the REFERENCE's own code.
+
+Runs oracle/_ref/neucor_ref — the reference's src/NeuCor.cpp compiled unmodified from
+its sources by oracle/Makefile — on small seeded scenarios and stores inputs and
+outputs.  Needs the reference tree (this script does not run on the GPU machines;
+its outputs are committed).
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import oracle as O  # noqa: E402
+from netgen import knn_net, random_net  # noqa: E402
+
+
+def params_dict(p):
+    return {f: np.asarray(getattr(p, f)) for f, _ in O.Params._fields_}
+
+
+def groups_arr(groups):
+    return np.array([[g["first"], g["count"], g["rate_hz"], g.get("correlated", 1), g.get("jitter", 2)]
+                     for g in groups], dtype=np.float64).reshape(-1, 5)
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print(name, os.path.getsize(path), "bytes")
+
+
+def scenario(name, mode, net, params, groups, steps, extra=(), record_pot=True, checkpoints=()):
+    xyz, pre, post, w = net
+    r = O.run_reference(mode, xyz, pre, post, w, params, groups=groups, steps=steps, record_pot=record_pot,
+                        extra_fires=list(extra), checkpoints=list(checkpoints) or [steps])
+    ex = np.asarray(list(extra), dtype=np.int32).reshape(-1, 2)
+    save(name, mode=np.asarray(mode), xyz=xyz, pre=pre, post=post, w=w, groups=groups_arr(groups), extra=ex,
+         steps=np.asarray(steps), checkpoints=np.asarray(list(checkpoints) or [steps], dtype=np.int32),
+         raster=r["raster"], pots=r["pots"] if record_pot else np.zeros(0, np.float32), weights=r["weights"],
+         pot=r["pot"], activity=r["activity"], last_fire=r["last_fire"], inhibitory=r["inhibitory"],
+         **{"p_" + k: v for k, v in params_dict(params).items()})
+
+
+def main():
+    if not O.reference_available():
+        O.build()
+    assert O.reference_available(), "needs the reference tree to build oracle/_ref"
+
+    # A. FEW_NEURONS preset through the reference's own API (src/main.cpp:162-189):
+    # 3 neurons, synapses 0->1, 0->2 at 0.5, periodic inputs at 50 Hz offset 0/+2/-2 ms,
+    # runAll, runSpeed 0.02, seed 1.  Weights at 50, 100, 150, 250 ms.
+    xyz = np.array([[0, 0, 0], [0.3, 0.3, 0], [0.3, -0.3, 0]], np.float32)
+    pre, post, w = np.array([0, 0], np.int32), np.array([1, 2], np.int32), np.array([0.5, 0.5], np.float32)
+    p = O.default_params(run_speed=0.02, seed=1)
+    firers = [dict(pos=tuple(map(float, xyz[i])), radius=0.1, rate_hz=50.0, offset_ms=[0.0, 2.0, -2.0][i])
+              for i in range(3)]
+    ck = [2500, 5000, 7500, 12500]
+    r = O.run_reference("continuous", xyz, pre, post, w, p, steps=12500, checkpoints=ck, firers=firers)
+    save("few_neurons_preset", checkpoints_ms=np.asarray(ck, np.float32) * np.float32(0.02), weights=r["weights"])
+
+    # B. canonical order: the reference's Neuron/Synapse code under a stepped scheduler
+    g1 = [dict(first=0, count=8, rate_hz=40.0, correlated=1, jitter=2),
+          dict(first=8, count=8, rate_hz=40.0, correlated=0)]
+    scenario("canonical_knn64", "canonical", knn_net(64, 6, 11, inhibitory=0.2), O.default_params(seed=5), g1, 400)
+    g2 = [dict(first=0, count=6, rate_hz=60.0, correlated=1, jitter=3)]
+    extra2 = [(t, (7 * t) % 40) for t in range(1, 300, 9)]
+    scenario("canonical_random40_dt05", "canonical", random_net(40, 300, 3),
+             O.default_params(seed=9, run_speed=0.5, learning_rate=0.7), g2, 300, extra=extra2)
+    extra3 = [(t, (13 * t) % 100) for t in range(1, 500, 4)]
+    scenario("canonical_knn100_nobg", "canonical", knn_net(100, 8, 12, weight_scale=0.6),
+             O.default_params(seed=2, background_firing=0), [], 500, extra=extra3, checkpoints=[100, 500])
+
+    # C. native order: the reference's own NeuCor::run with runAll (bit-exact until the
+    # first same-step coincidence whose order the reference leaves to its heap)
+    g4 = [dict(first=0, count=10, rate_hz=10.0, correlated=1, jitter=2),
+          dict(first=10, count=10, rate_hz=10.0, correlated=0)]
+    net = knn_net(200, 6, 0, weight_scale=0.25)
+    xyz, pre, post, w = net
+    p4 = O.default_params(seed=77)
+    r = O.run_reference("native", xyz, pre, post, w, p4, groups=g4, steps=1000, record_pot=True)
+    save("native_knn200", xyz=xyz, pre=pre, post=post, w=w, groups=groups_arr(g4), steps=np.asarray(1000),
+         raster=r["raster"], inhibitory=r["inhibitory"], pots_every50=r["pots"][49::50], **{"p_" + k: v for k, v in params_dict(p4).items()})
+
+    # D. the reference constructor NeuCor(60) after srand(3)
+    xyz, fr, to, w, ln = O.reference_construct(60, 3)
+    save("construct_n60_seed3", xyz=xyz, pre=fr, post=to, w=w, length=ln)
+
+
+if __name__ == "__main__":
+    main()
