@@ -360,7 +360,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--sim-steps-per-step", type=int, default=SIM_STEPS_PER_STEP,
+                    help="simulation steps per bench step (smaller values make ncu-sized cases)")
     args = ap.parse_args()
+    globals()["SIM_STEPS_PER_STEP"] = args.sim_steps_per_step
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":

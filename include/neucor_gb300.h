@@ -196,17 +196,73 @@ int nc_delete_neuron(nc_net* net, int32_t id);
  * from/to/weight (n*k).  Lengths follow coord3::getDist (src/NeuCor.h:16-18). */
 int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, float* xyz, int32_t* syn_from,
                  int32_t* syn_to, float* syn_weight);
-/* nc_build_reference_random: the reference constructor NeuCor(n) (src/NeuCor.cpp:17-42):
- * sphere placement (src/NeuCor.cpp:154-170) and radius-1 connection of every ordered
- * pair (src/NeuCor.cpp:418-444) with weights rand()*0.8+0.2, 20% negated
- * (src/NeuCor.cpp:471-473), drawing from the C library's rand() in the reference's
- * order — so after srand(s) it builds the network the reference builds after srand(s).
- * Pass NULL outputs to get *n_synapses first. */
-int nc_build_reference_random(int32_t n, float* xyz, int32_t* syn_from, int32_t* syn_to, float* syn_weight,
-                              int64_t capacity, int64_t* n_synapses);
+/* The reference constructor NeuCor(n) (src/NeuCor.cpp:17-42) in three calls that draw
+ * from the C library's rand() in the reference's order, so after srand(s) they build
+ * the network the reference builds after srand(s):
+ *   nc_reference_positions: createNeuron with random positions in a sphere
+ *     (src/NeuCor.cpp:154-170), 3*n floats (draws rand());
+ *   nc_reference_connection_count: pairs closer than 1 unit (src/NeuCor.cpp:418-444),
+ *     no draws;
+ *   nc_reference_connections: those pairs in the reference's order with weights
+ *     rand()*0.8+0.2, 20% negated (src/NeuCor.cpp:471-473) (draws rand()). */
+int nc_reference_positions(int32_t n, float* xyz);
+int nc_reference_connection_count(int32_t n, const float* xyz, int64_t* n_synapses);
+int nc_reference_connections(int32_t n, const float* xyz, int32_t* syn_from, int32_t* syn_to, float* syn_weight,
+                             int64_t capacity);
 
 /* Philox4x32-10 (Salmon et al., SC'11), the counter-based generator behind every draw. */
 int nc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* ------------------------------------------------------ batched networks */
+/* Many independent networks packed into one device engine and advanced together:
+ * every launch pair steps every unfinished network once.  Each network keeps its own
+ * constants, seed, inputs and horizon, and no state is shared, so a network computes
+ * the same bits alone (nc_create) or packed.  There is no reference counterpart: the
+ * reference simulates one NeuCor at a time (src/NeuCor.cpp:583-617). */
+typedef struct nc_batch nc_batch;
+
+typedef struct {
+    int32_t n_neurons;
+    const float* xyz;            /* 3*n; may be NULL if syn_length is given */
+    int64_t n_synapses;
+    const int32_t* syn_from;
+    const int32_t* syn_to;
+    const float* syn_weight;
+    const float* syn_length;     /* may be NULL */
+    const uint8_t* syn_inhibitory; /* may be NULL */
+    nc_params params;
+    int32_t n_groups;
+    const nc_group* groups;
+    int32_t horizon;             /* steps to simulate; the network idles afterwards */
+} nc_net_spec;
+
+/* Launch configuration of an engine (the autotuner's search space). */
+typedef struct {
+    int32_t neuron_block;        /* threads per block of the neuron update (multiple of 32) */
+    int32_t launch_blocks;       /* blocks of the spike launch */
+    int32_t launch_block;        /* threads per block of the spike launch */
+    int32_t graph_steps;         /* launch pairs per captured CUDA graph */
+} nc_launch_config;
+
+int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out);
+int nc_batch_destroy(nc_batch* batch);
+/* Advances every unfinished network by up to `steps` steps. */
+int nc_batch_run(nc_batch* batch, int32_t steps);
+/* Same, timed with CUDA events on the engine's stream (ms of device time). */
+int nc_batch_time(nc_batch* batch, int32_t steps, float* ms);
+/* Runs until every network reached its horizon. */
+int nc_batch_run_to_end(nc_batch* batch);
+int nc_batch_get_launch(nc_batch* batch, nc_launch_config* out);
+int nc_batch_set_launch(nc_batch* batch, const nc_launch_config* cfg);
+/* Times `steps_per_trial` steps under each candidate configuration (the simulation
+ * advances during the trials; results do not depend on the configuration) and keeps
+ * the fastest; *best receives it. */
+int nc_batch_autotune(nc_batch* batch, int32_t steps_per_trial, nc_launch_config* best);
+int nc_batch_get_stats(nc_batch* batch, int32_t net, nc_stats* out);
+int nc_batch_get_step(nc_batch* batch, int32_t net, int64_t* step);
+int nc_batch_read_potentials(nc_batch* batch, int32_t net, float* out_n);
+int nc_batch_read_weights(nc_batch* batch, int32_t net, float* out_s);
+int nc_batch_read_last_fire(nc_batch* batch, int32_t net, float* out_n);
 
 /* Times n_steps of the handle's step kernels with CUDA events on its stream;
  * *ms receives the elapsed device time, *kernel_ms (may be NULL) two entries:

@@ -63,6 +63,21 @@ class SynapseSnapshotC(ctypes.Structure):
                 ("pre_potential", ctypes.c_float), ("post_potential", ctypes.c_float), ("inhibitory", ctypes.c_int32)]
 
 
+class NetSpec(ctypes.Structure):
+    _fields_ = [("n_neurons", ctypes.c_int32), ("xyz", ctypes.c_void_p), ("n_synapses", ctypes.c_int64),
+                ("syn_from", ctypes.c_void_p), ("syn_to", ctypes.c_void_p), ("syn_weight", ctypes.c_void_p),
+                ("syn_length", ctypes.c_void_p), ("syn_inhibitory", ctypes.c_void_p), ("params", Params),
+                ("n_groups", ctypes.c_int32), ("groups", ctypes.c_void_p), ("horizon", ctypes.c_int32)]
+
+
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("neuron_block", ctypes.c_int32), ("launch_blocks", ctypes.c_int32), ("launch_block", ctypes.c_int32),
+                ("graph_steps", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -96,8 +111,15 @@ def load_library() -> ctypes.CDLL:
         "nc_get_stats": ([P, P], I32), "nc_delete_synapse": ([P, I32, I32], I32),
         "nc_delete_neuron": ([P, I32], I32),
         "nc_build_knn": ([I32, I32, F, ctypes.c_uint64, P, P, P, P], I32),
-        "nc_build_reference_random": ([I32, P, P, P, P, I64, P], I32),
+        "nc_reference_positions": ([I32, P], I32), "nc_reference_connection_count": ([I32, P, P], I32),
+        "nc_reference_connections": ([I32, P, P, P, P, I64], I32),
         "nc_philox4x32_10": ([P, P, P], I32), "nc_time_steps": ([P, I32, P, P], I32),
+        "nc_batch_create": ([I32, P, P], I32), "nc_batch_destroy": ([P], I32), "nc_batch_run": ([P, I32], I32),
+        "nc_batch_time": ([P, I32, P], I32), "nc_batch_run_to_end": ([P], I32),
+        "nc_batch_get_launch": ([P, P], I32), "nc_batch_set_launch": ([P, P], I32),
+        "nc_batch_autotune": ([P, I32, P], I32), "nc_batch_get_stats": ([P, I32, P], I32),
+        "nc_batch_get_step": ([P, I32, P], I32), "nc_batch_read_potentials": ([P, I32, P], I32),
+        "nc_batch_read_weights": ([P, I32, P], I32), "nc_batch_read_last_fire": ([P, I32, P], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -158,15 +180,15 @@ def build_reference_random(n: int, seed: int):
     libc = ctypes.CDLL(None)
     libc.srand(ctypes.c_uint(seed))
     L = load_library()
-    cnt = ctypes.c_int64(0)
-    _check(L.nc_build_reference_random(n, None, None, None, None, 0, ctypes.byref(cnt)))
-    libc.srand(ctypes.c_uint(seed))
     xyz = np.zeros((n, 3), dtype=np.float32)
+    _check(L.nc_reference_positions(n, _p(xyz)))
+    cnt = ctypes.c_int64(0)
+    _check(L.nc_reference_connection_count(n, _p(xyz), ctypes.byref(cnt)))
     s = cnt.value
     pre = np.zeros(s, dtype=np.int32)
     post = np.zeros(s, dtype=np.int32)
     w = np.zeros(s, dtype=np.float32)
-    _check(L.nc_build_reference_random(n, _p(xyz), _p(pre), _p(post), _p(w), s, ctypes.byref(cnt)))
+    _check(L.nc_reference_connections(n, _p(xyz), _p(pre), _p(post), _p(w), s))
     return xyz, pre, post, w
 
 
@@ -488,3 +510,104 @@ class NeuCor:
 
 def _nan_to_none(v):
     return None if (isinstance(v, float) and math.isnan(v)) else v
+
+
+class Batch:
+    """Many independent networks advanced together in one device engine (nc_batch_*).
+
+    ``nets`` is a list of dicts: xyz, pre, post, weight (arrays), and optionally length,
+    inhibitory, params (Params), groups (list of dicts), horizon (steps)."""
+
+    def __init__(self, nets):
+        self._lib = load_library()
+        self._keep = []
+        specs = (NetSpec * len(nets))()
+        self.n_input = []
+        for q, d in enumerate(nets):
+            xyz = np.ascontiguousarray(d["xyz"], dtype=np.float32).reshape(-1, 3)
+            pre = np.ascontiguousarray(d["pre"], dtype=np.int32)
+            post = np.ascontiguousarray(d["post"], dtype=np.int32)
+            w = np.ascontiguousarray(d["weight"], dtype=np.float32)
+            ln = d.get("length")
+            ln = None if ln is None else np.ascontiguousarray(ln, dtype=np.float32)
+            inh = d.get("inhibitory")
+            inh = None if inh is None else np.ascontiguousarray(inh, dtype=np.uint8)
+            groups = d.get("groups", [])
+            garr = (Group * max(1, len(groups)))()
+            for i, g in enumerate(groups):
+                garr[i] = Group(int(g["first"]), int(g["count"]), float(g["rate_hz"]), int(g.get("correlated", 1)),
+                                int(g.get("jitter", 2)))
+            self._keep += [xyz, pre, post, w, ln, inh, garr]
+            specs[q] = NetSpec(xyz.shape[0], _p(xyz), pre.shape[0], _p(pre), _p(post), _p(w), _p(ln), _p(inh),
+                               d.get("params") or default_params(), len(groups), ctypes.cast(garr, ctypes.c_void_p),
+                               int(d.get("horizon", 1 << 30)))
+            self.n_input.append(pre.shape[0])
+        self.sizes = [int(np.asarray(d["xyz"]).reshape(-1, 3).shape[0]) for d in nets]
+        h = ctypes.c_void_p()
+        _check(self._lib.nc_batch_create(len(nets), ctypes.cast(specs, ctypes.c_void_p), ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, steps: int):
+        _check(self._lib.nc_batch_run(self._h, int(steps)))
+
+    def time(self, steps: int) -> float:
+        ms = ctypes.c_float()
+        _check(self._lib.nc_batch_time(self._h, int(steps), ctypes.byref(ms)))
+        return float(ms.value)
+
+    def run_to_end(self):
+        _check(self._lib.nc_batch_run_to_end(self._h))
+
+    def launch(self) -> dict:
+        c = LaunchConfig()
+        _check(self._lib.nc_batch_get_launch(self._h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def set_launch(self, **kw):
+        c = LaunchConfig()
+        _check(self._lib.nc_batch_get_launch(self._h, ctypes.byref(c)))
+        for k, v in kw.items():
+            setattr(c, k, int(v))
+        _check(self._lib.nc_batch_set_launch(self._h, ctypes.byref(c)))
+
+    def autotune(self, steps_per_trial: int = 50) -> dict:
+        c = LaunchConfig()
+        _check(self._lib.nc_batch_autotune(self._h, int(steps_per_trial), ctypes.byref(c)))
+        return c.as_dict()
+
+    def stats(self, net: int) -> dict:
+        s = _Stats()
+        _check(self._lib.nc_batch_get_stats(self._h, int(net), ctypes.byref(s)))
+        return {f: int(getattr(s, f)) for f, _ in _Stats._fields_}
+
+    def step(self, net: int) -> int:
+        v = ctypes.c_int64()
+        _check(self._lib.nc_batch_get_step(self._h, int(net), ctypes.byref(v)))
+        return int(v.value)
+
+    def potentials(self, net: int):
+        out = np.zeros(self.sizes[net], dtype=np.float32)
+        _check(self._lib.nc_batch_read_potentials(self._h, int(net), _p(out)))
+        return out
+
+    def weights(self, net: int):
+        out = np.zeros(self.n_input[net], dtype=np.float32)
+        _check(self._lib.nc_batch_read_weights(self._h, int(net), _p(out)))
+        return out
+
+    def lastFire(self, net: int):
+        out = np.zeros(self.sizes[net], dtype=np.float32)
+        _check(self._lib.nc_batch_read_last_fire(self._h, int(net), _p(out)))
+        return out

@@ -15,6 +15,11 @@ int fail(int code, const std::string& msg)
     g_err = msg;
     return code;
 }
+}  // namespace
+
+int nc::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
+namespace {
 
 // AP_RENDER_BEHAVIOUR (src/NeuCor.cpp:547-550)
 float render_behaviour(float val)

@@ -376,13 +376,14 @@ extern "C" int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, 
     return NC_OK;
 }
 
-extern "C" int nc_build_reference_random(int32_t n, float* xyz, int32_t* syn_from, int32_t* syn_to,
-                                         float* syn_weight, int64_t capacity, int64_t* n_synapses)
+namespace {
+float randomUnit() { return static_cast<float>(rand()) / static_cast<float>(RAND_MAX); }
+}  // namespace
+
+extern "C" int nc_reference_positions(int32_t n, float* xyz)
 {
-    if (n < 0 || !n_synapses) return NC_ERR_INVALID;
-    auto randomUnit = []() { return static_cast<float>(rand()) / static_cast<float>(RAND_MAX); };
+    if (n < 0 || (n > 0 && !xyz)) return NC_ERR_INVALID;
     // createNeuron with NaN positions while totalGenNeurons = n (src/NeuCor.cpp:154-170)
-    std::vector<float> pos(3 * (size_t)n);
     float spawnSize = 2.0f;
     if (n != 0) spawnSize = powf((float)((unsigned)n / (1.3333 * 3.1459 * 8)), (float)0.33333) * 2.0;
     for (int32_t i = 0; i < n; ++i) {
@@ -392,28 +393,43 @@ extern "C" int nc_build_reference_random(int32_t n, float* xyz, int32_t* syn_fro
             y = (randomUnit() - 0.5f) * spawnSize;
             z = (randomUnit() - 0.5f) * spawnSize;
         } while ((double)x * x + (double)y * y + (double)z * z > (spawnSize / 2.0) * (spawnSize / 2.0));
-        pos[3 * (size_t)i] = x;
-        pos[3 * (size_t)i + 1] = y;
-        pos[3 * (size_t)i + 2] = z;
+        xyz[3 * (size_t)i] = x;
+        xyz[3 * (size_t)i + 1] = y;
+        xyz[3 * (size_t)i + 2] = z;
     }
-    if (xyz) std::memcpy(xyz, pos.data(), sizeof(float) * pos.size());
-    // Neuron::makeConnections for every neuron in order (src/NeuCor.cpp:418-444); each
-    // new Synapse draws its weight (src/NeuCor.cpp:471-473)
+    return NC_OK;
+}
+
+extern "C" int nc_reference_connection_count(int32_t n, const float* xyz, int64_t* n_synapses)
+{
+    if (n < 0 || !n_synapses || (n > 0 && !xyz)) return NC_ERR_INVALID;
     int64_t s = 0;
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = 0; j < n; ++j)
+            if (nc::get_dist(&xyz[3 * (size_t)i], &xyz[3 * (size_t)j]) < 1.0 && j != i) ++s;
+    *n_synapses = s;
+    return NC_OK;
+}
+
+extern "C" int nc_reference_connections(int32_t n, const float* xyz, int32_t* syn_from, int32_t* syn_to,
+                                        float* syn_weight, int64_t capacity)
+{
+    if (n < 0 || (n > 0 && !xyz)) return NC_ERR_INVALID;
+    int64_t s = 0;
+    // Neuron::makeConnections for every neuron in order (src/NeuCor.cpp:418-444); each new
+    // Synapse draws its weight (src/NeuCor.cpp:471-473)
     for (int32_t i = 0; i < n; ++i) {
         for (int32_t j = 0; j < n; ++j) {
-            const float distance = nc::get_dist(&pos[3 * (size_t)i], &pos[3 * (size_t)j]);
+            const float distance = nc::get_dist(&xyz[3 * (size_t)i], &xyz[3 * (size_t)j]);
             if (!(distance < 1.0 && j != i)) continue;
+            if (s >= capacity || !syn_from || !syn_to || !syn_weight) return NC_ERR_INVALID;
             float weight = randomUnit() * 0.8f + 0.2f;
             if (randomUnit() < 0.2f) weight = -weight;
-            if (syn_from && s < capacity) {
-                syn_from[s] = i;
-                syn_to[s] = j;
-                syn_weight[s] = weight;
-            }
+            syn_from[s] = i;
+            syn_to[s] = j;
+            syn_weight[s] = weight;
             ++s;
         }
     }
-    *n_synapses = s;
-    return (syn_from && s > capacity) ? NC_ERR_INVALID : NC_OK;
+    return NC_OK;
 }

@@ -77,7 +77,15 @@ static cudaError_t upload(T* dev, const std::vector<T>& host, size_t offset, cud
     return cudaMemcpyAsync(dev + offset, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, s);
 }
 
-int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err)
+void Engine::set_launch(const LaunchShape& shape, int ticks_per_graph)
+{
+    release_graph();
+    L = shape;
+    graph_ticks = ticks_per_graph;
+}
+
+int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err,
+                  const std::vector<int32_t>* horizons)
 {
     NC_CK(cudaGetDevice(&device));
     NC_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -109,7 +117,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         NcNetDesc d;
         std::memset(&d, 0, sizeof(d));
         d.t = 1;
-        d.t_end = 1 << 30;
+        d.t_end = horizons ? (*horizons)[q] : (1 << 30);
         d.stdp_done = 0;
         d.n = h.n;
         d.neuron_base = sl.neuron_base;
@@ -371,6 +379,9 @@ int Engine::set_groups(int net, const std::vector<NcGroupDev>& groups, std::stri
 
 int Engine::set_rates(int net, float lr, float pre_factor, float post_factor, std::string& err)
 {
+    // plasticity still pending from the last step belongs to the old rates
+    const int rc = flush_plasticity(err);
+    if (rc != NC_OK) return rc;
     NC_CK(put_field(P.nets, net, offsetof(NcNetDesc, lr), lr, stream));
     NC_CK(put_field(P.nets, net, offsetof(NcNetDesc, pre_factor), pre_factor, stream));
     NC_CK(put_field(P.nets, net, offsetof(NcNetDesc, post_factor), post_factor, stream));

@@ -29,7 +29,9 @@ public:
 
     // Packs the nets (all starting at step 1) and uploads them.  group_capacity is
     // the number of input-group entries reserved per net.
-    int build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err);
+    int build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err,
+              const std::vector<int32_t>* horizons = nullptr);
+    void set_launch(const LaunchShape& shape, int ticks_per_graph);
     // Runs `ticks` engine steps (every active net advances one step per tick).
     int step(int64_t ticks, std::string& err);
     // Same, timed with CUDA events on the engine stream.
@@ -70,5 +72,7 @@ private:
 };
 
 std::string cuda_msg(const char* what, cudaError_t e);
+// Records the calling thread's last error (nc_last_error) and returns `code`.
+int set_last_error(int code, const std::string& msg);
 
 }  // namespace nc
