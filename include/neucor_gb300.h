@@ -64,7 +64,18 @@ typedef struct {
     int32_t background_firing;      /* 1: random background fires every step (src/NeuCor.cpp:604-607); 0: off */
     int32_t inhibitory_rule;        /* NC_INHIBITORY_* below */
     uint64_t seed;                  /* key of the counter-based draws (background, inputs) */
+    int32_t storage_order;          /* NC_ORDER_*: how neurons are laid out in device memory */
+    int32_t reserved;
 } nc_params;
+
+/* Device layout of neurons.  Results never depend on it (ids, the in-synapse fold
+ * order and the same-step order rules all use the caller's ids).
+ *   NC_ORDER_SPATIAL  Morton order of the positions (default): a neuron's targets sit
+ *                     near it in memory, so the scattered accesses of a step share cache
+ *                     lines;
+ *   NC_ORDER_ID       the caller's id order. */
+#define NC_ORDER_SPATIAL 0
+#define NC_ORDER_ID 1
 
 /* A group of input neurons driven by Poisson spike trains.  Members are the
  * neurons first .. first+count-1.  Correlated groups share one source whose every
@@ -238,9 +249,9 @@ typedef struct {
 
 /* Launch configuration of an engine (the autotuner's search space). */
 typedef struct {
-    int32_t neuron_block;        /* threads per block of the neuron update (multiple of 32) */
+    int32_t neuron_block;        /* threads per block of the neuron update (32..256, multiple of 32) */
     int32_t launch_blocks;       /* blocks of the spike launch */
-    int32_t launch_block;        /* threads per block of the spike launch */
+    int32_t launch_block;        /* threads per block of the spike launch (32..256, multiple of 32) */
     int32_t graph_steps;         /* launch pairs per captured CUDA graph */
 } nc_launch_config;
 

@@ -45,6 +45,8 @@ class Params(ctypes.Structure):
         ("background_firing", ctypes.c_int32),
         ("inhibitory_rule", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
+        ("storage_order", ctypes.c_int32),
+        ("reserved2", ctypes.c_int32),
     ]
 
 

@@ -189,9 +189,12 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* ids)
 {
     NC_NEED(net);
     if (count < 0 || (count > 0 && !ids)) return fail(NC_ERR_INVALID, "bad id array");
-    for (int32_t k = 0; k < count; ++k)
+    std::vector<int32_t> slots((size_t)count);
+    for (int32_t k = 0; k < count; ++k) {
         if (ids[k] < 0 || ids[k] >= net->host.n) return fail(NC_ERR_INVALID, "neuron id out of range");
-    NC_CALL(net->eng, force_fire, 0, ids, count);
+        slots[(size_t)k] = net->host.slot_of[(size_t)ids[k]];
+    }
+    NC_CALL(net->eng, force_fire, 0, slots.data(), count);
     return NC_OK;
 }
 
@@ -271,8 +274,21 @@ int nc_read_raster(nc_net* net, uint8_t* out, int64_t capacity_bytes, int32_t* s
     if (capacity_bytes < rows * row_bytes) return fail(NC_ERR_INVALID, "raster buffer too small");
     std::vector<uint32_t> buf((size_t)rows * nw);
     NC_CALL(net->eng, download, buf.data(), (const uint32_t*)net->d_raster, buf.size());
-    for (int32_t r = 0; r < rows; ++r)
-        std::memcpy(out + (int64_t)r * row_bytes, buf.data() + (size_t)r * nw, (size_t)row_bytes);
+    const nc::NetHost& h = net->host;
+    for (int32_t r = 0; r < rows; ++r) {
+        uint8_t* o = out + (int64_t)r * row_bytes;
+        const uint32_t* b = buf.data() + (size_t)r * nw;
+        if (!h.permuted) {
+            std::memcpy(o, b, (size_t)row_bytes);
+            continue;
+        }
+        std::memset(o, 0, (size_t)row_bytes);
+        for (int32_t s = 0; s < h.n; ++s)
+            if ((b[s >> 5] >> (s & 31)) & 1u) {
+                const int32_t i = h.orig_id[(size_t)s];
+                o[i >> 3] |= (uint8_t)(1u << (i & 7));
+            }
+    }
     return NC_OK;
 }
 
@@ -281,7 +297,9 @@ int nc_read_potentials(nc_net* net, float* out_n)
     NC_NEED(net);
     if (!out_n && net->host.n) return fail(NC_ERR_INVALID, "null output");
     const auto& sl = net->eng.slots[0];
-    NC_CALL(net->eng, download, out_n, (const float*)net->eng.P.pot + sl.neuron_base, (size_t)sl.n);
+    std::vector<float> pot((size_t)sl.n);
+    NC_CALL(net->eng, download, pot.data(), (const float*)net->eng.P.pot + sl.neuron_base, (size_t)sl.n);
+    nc::to_caller_order(net->host, pot.data(), out_n);
     return NC_OK;
 }
 
@@ -299,6 +317,15 @@ int nc_read_potact(nc_net* net, float* out_2n)
     NC_CALL(net->eng, download, start.data(), (const int32_t*)net->eng.P.act_start + sl.neuron_base, (size_t)n);
     const float dt = net->host.dt;
     const int64_t t = net->step;
+    std::vector<float> pot_c((size_t)n);
+    std::vector<uint32_t> fir_c((size_t)n);
+    std::vector<int32_t> start_c((size_t)n);
+    nc::to_caller_order(net->host, pot.data(), pot_c.data());
+    nc::to_caller_order(net->host, fir.data(), fir_c.data());
+    nc::to_caller_order(net->host, start.data(), start_c.data());
+    pot.swap(pot_c);
+    fir.swap(fir_c);
+    start.swap(start_c);
     for (int32_t j = 0; j < n; ++j) {
         out_2n[2 * (size_t)j] = pot[j];
         // setActivity(firings/(((float) currentT-activityStartTime)/10.0)) at the last update
@@ -322,8 +349,9 @@ int nc_read_last_fire(nc_net* net, float* out_n)
     NC_NEED(net);
     const int32_t n = net->host.n;
     if (!out_n && n) return fail(NC_ERR_INVALID, "null output");
-    std::vector<int32_t> lf((size_t)n);
-    NC_CALL(net->eng, download, lf.data(), (const int32_t*)net->eng.P.lf + net->eng.slots[0].neuron_base, (size_t)n);
+    std::vector<int32_t> lf_s((size_t)n), lf((size_t)n);
+    NC_CALL(net->eng, download, lf_s.data(), (const int32_t*)net->eng.P.lf + net->eng.slots[0].neuron_base, (size_t)n);
+    nc::to_caller_order(net->host, lf_s.data(), lf.data());
     for (int32_t j = 0; j < n; ++j) out_n[j] = lf[j] == NC_NEVER ? NAN : nc::step_ms(lf[j], net->host.dt);
     return NC_OK;
 }
@@ -388,12 +416,14 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
     NC_CALL(net->eng, download, optr.data(), (const int64_t*)P.out_ptr + sl.ptr_base, (size_t)h.n + 1);
     const float T = net->time;
     const int64_t t = net->step;
+    int64_t q = 0;
     for (int32_t i = 0; i < h.n; ++i) {
-        for (int64_t k = optr[i] - sl.syn_base; k < optr[i + 1] - sl.syn_base; ++k) {
-            nc_synapse_snapshot& o = out[k];
+        const int32_t si = h.slot_of[(size_t)i];
+        for (int64_t k = optr[si] - sl.syn_base; k < optr[si + 1] - sl.syn_base; ++k) {
+            nc_synapse_snapshot& o = out[q++];
             const float weight = w[(size_t)csc[(size_t)k]];
             o.from_id = i;
-            o.to_id = post[(size_t)k];
+            o.to_id = h.orig_id[(size_t)post[(size_t)k]];
             o.weight = weight;
             o.inhibitory = weight < 0.0f;
             o.pre_potential = 0.0f;
@@ -401,7 +431,7 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
             const int32_t a = la[(size_t)k];
             // in flight (AP_fireTime != 0) until its target's update KC steps after arrival
             if (a == NC_NEVER || t - a >= h.kc) continue;
-            const int32_t d = dly[(size_t)k];
+            const int32_t d = (int32_t)((uint16_t)dly[(size_t)k] & 0x3fffu);
             const float length_speed = ((float)d * h.dt / 2.0f) * 2.0f;  // length*AP_speed
             const float fire_time = nc::step_ms(a, h.dt);                  // AP_fireTime
             const float start = nc::step_ms(a - d, h.dt);                  // lastSpikeStart

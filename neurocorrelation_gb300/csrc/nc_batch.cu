@@ -162,9 +162,11 @@ int nc_batch_get_launch(nc_batch* b, nc_launch_config* out)
 int nc_batch_set_launch(nc_batch* b, const nc_launch_config* c)
 {
     B_NEED(b);
-    if (!c || c->neuron_block < 32 || c->neuron_block > 1024 || c->neuron_block % 32 || c->launch_block < 32 ||
-        c->launch_block > 1024 || c->launch_block % 32 || c->launch_blocks < 1 || c->graph_steps < 0)
-        return bfail(NC_ERR_INVALID, "bad launch configuration");
+    // the step kernels are compiled for at most 256 threads per block
+    if (!c || c->neuron_block < 32 || c->neuron_block > 256 || c->neuron_block % 32 || c->launch_block < 32 ||
+        c->launch_block > 256 || c->launch_block % 32 || c->launch_blocks < 1 || c->launch_blocks > (1 << 20) ||
+        c->graph_steps < 0 || c->graph_steps > 4096)
+        return bfail(NC_ERR_INVALID, "bad launch configuration (blocks of 32..256 threads)");
     B_CALL0(b->eng, sync);
     nc::LaunchShape L{c->neuron_block, c->launch_blocks, c->launch_block};
     b->eng.set_launch(L, c->graph_steps);
@@ -178,7 +180,7 @@ int nc_batch_autotune(nc_batch* b, int32_t steps_per_trial, nc_launch_config* be
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->eng.device);
     std::vector<nc_launch_config> cands;
-    for (int nb : {128, 256, 512})
+    for (int nb : {64, 128, 256})
         for (int lbm : {2, 4, 8})
             for (int lb : {128, 256})
                 for (int g : {16, 64}) cands.push_back(nc_launch_config{nb, sms * lbm, lb, g});
@@ -228,7 +230,9 @@ int nc_batch_read_potentials(nc_batch* b, int32_t net, float* out)
     B_NEED(b);
     if (!out || net < 0 || net >= (int32_t)b->hosts.size()) return bfail(NC_ERR_INVALID, "bad net index");
     const auto& sl = b->eng.slots[(size_t)net];
-    B_CALL(b->eng, download, out, (const float*)b->eng.P.pot + sl.neuron_base, (size_t)sl.n);
+    std::vector<float> pot((size_t)sl.n);
+    B_CALL(b->eng, download, pot.data(), (const float*)b->eng.P.pot + sl.neuron_base, (size_t)sl.n);
+    nc::to_caller_order(b->hosts[(size_t)net], pot.data(), out);
     return NC_OK;
 }
 
@@ -254,8 +258,9 @@ int nc_batch_read_last_fire(nc_batch* b, int32_t net, float* out)
     B_NEED(b);
     if (!out || net < 0 || net >= (int32_t)b->hosts.size()) return bfail(NC_ERR_INVALID, "bad net index");
     const auto& sl = b->eng.slots[(size_t)net];
-    std::vector<int32_t> lf((size_t)sl.n);
-    B_CALL(b->eng, download, lf.data(), (const int32_t*)b->eng.P.lf + sl.neuron_base, (size_t)sl.n);
+    std::vector<int32_t> lf_s((size_t)sl.n), lf((size_t)sl.n);
+    B_CALL(b->eng, download, lf_s.data(), (const int32_t*)b->eng.P.lf + sl.neuron_base, (size_t)sl.n);
+    nc::to_caller_order(b->hosts[(size_t)net], lf_s.data(), lf.data());
     for (int32_t j = 0; j < sl.n; ++j) out[j] = lf[(size_t)j] == NC_NEVER ? NAN : nc::step_ms(lf[(size_t)j], sl.dt);
     return NC_OK;
 }

@@ -14,7 +14,11 @@
 //                           contribution term captured at launch (double)
 //   inh                     one bit per in-synapse: Synapse::inhibitory
 //   out_ptr   CSR row starts (n+1) and per out-synapse (CSR order): target,
-//             CSC index, delay, ring bit position, last accepted arrival step
+//             CSC index, delay (bits 0-13; bit 14/15: the target's caller id is
+//             above/below the source's), ring bit position, last accepted arrival step
+//   Neurons sit in device slots (Morton order of positions by default); every rule
+//   that depends on ids uses the caller's ids (orig_id, the out_delay flags, the
+//   in-synapse order).
 //   ring      R slots x W words: bit b of target j's words in slot a mod R set when
 //             the spike on j's b-th in-synapse arrives at step a
 //   fired / forced   two parities of one bit per neuron
@@ -70,7 +74,7 @@ struct NcNetDesc {
     int32_t active;       // 0: skipped by the kernels
     int32_t raster_len;   // recorded steps capacity (0 = off)
     int32_t raster_t0;    // first recorded step
-    int32_t pad0;
+    int32_t permuted;     // neurons are stored in a different order than the caller's ids
     float dt;
     float leak;           // powf(0.5f, dt)  (src/NeuCor.cpp:678)
     float c52;            // float(0.2f * 52.0) (src/NeuCor.cpp:729-730)
@@ -91,6 +95,8 @@ struct NcPools {
     int32_t* lf;
     uint32_t* firings;
     int32_t* act_start;
+    int32_t* orig_id;    // device slot -> caller's id (local to the net)
+    int32_t* slot_of;    // caller's id -> device slot (local to the net)
     // per-neuron pointers (n+1 per net)
     int64_t* in_ptr;     // absolute CSC index
     int64_t* out_ptr;    // absolute CSR index

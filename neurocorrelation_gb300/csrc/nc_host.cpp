@@ -54,6 +54,58 @@ float ap_value(float x)
     return (float)v;
 }
 
+// Morton code of a position quantised to 10 bits per axis over the bounding box.
+static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z)
+{
+    auto spread = [](uint32_t v) {
+        v &= 0x3ffu;
+        v = (v | (v << 16)) & 0x30000ffu;
+        v = (v | (v << 8)) & 0x300f00fu;
+        v = (v | (v << 4)) & 0x30c30c3u;
+        v = (v | (v << 2)) & 0x9249249u;
+        return v;
+    };
+    return spread(x) | (spread(y) << 1) | (spread(z) << 2);
+}
+
+static void storage_order(NetHost& h, const float* xyz, int32_t order_kind)
+{
+    const int32_t n = h.n;
+    h.orig_id.resize((size_t)n);
+    h.slot_of.resize((size_t)n);
+    for (int32_t i = 0; i < n; ++i) h.orig_id[(size_t)i] = i;
+    if (order_kind == NC_ORDER_SPATIAL && xyz && n > 1) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int32_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double v = xyz[3 * (size_t)i + a];
+                if (std::isfinite(v)) {
+                    lo[a] = std::min(lo[a], v);
+                    hi[a] = std::max(hi[a], v);
+                }
+            }
+        std::vector<uint32_t> code((size_t)n);
+        for (int32_t i = 0; i < n; ++i) {
+            uint32_t q[3];
+            for (int a = 0; a < 3; ++a) {
+                const double v = xyz[3 * (size_t)i + a];
+                const double span = hi[a] - lo[a];
+                double f = (std::isfinite(v) && span > 0) ? (v - lo[a]) / span : 0.0;
+                f = std::min(1.0, std::max(0.0, f));
+                q[a] = (uint32_t)(f * 1023.0);
+            }
+            code[(size_t)i] = morton3(q[0], q[1], q[2]);
+        }
+        std::stable_sort(h.orig_id.begin(), h.orig_id.end(),
+                         [&](int32_t a, int32_t b) { return code[(size_t)a] < code[(size_t)b]; });
+    }
+    h.permuted = false;
+    for (int32_t s = 0; s < n; ++s) {
+        h.slot_of[(size_t)h.orig_id[(size_t)s]] = s;
+        if (h.orig_id[(size_t)s] != s) h.permuted = true;
+    }
+}
+
 int64_t NetHost::device_bytes() const
 {
     const int64_t per_neuron = 4 + 4 + 4 + 4 + 8 + 8 + 4;             // pot lf firings act_start in_ptr out_ptr ring_off
@@ -131,16 +183,22 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
     h.e_term = exp(0.3702 * (double)h.dt);              // exp(0.3702*deltaT)
     h.xyz.assign(3 * (size_t)n, 0.0f);
     if (xyz) std::memcpy(h.xyz.data(), xyz, sizeof(float) * 3 * (size_t)n);
+    if (p.storage_order != NC_ORDER_SPATIAL && p.storage_order != NC_ORDER_ID) {
+        err = "unknown storage order";
+        return NC_ERR_INVALID;
+    }
+    storage_order(h, xyz, p.storage_order);
 
-    // CSC: bucket by target in input order, sort each bucket by source (stable), keep
-    // the first of repeated (source, target) pairs (createSynapse, src/NeuCor.cpp:189-191)
+    // CSC: bucket by target slot in input order, sort each bucket by the caller's source
+    // id (stable), keep the first of repeated (source, target) pairs (createSynapse,
+    // src/NeuCor.cpp:189-191)
     std::vector<int64_t> bstart((size_t)n + 1, 0);
-    for (int64_t k = 0; k < n_syn; ++k) bstart[(size_t)to[k] + 1]++;
+    for (int64_t k = 0; k < n_syn; ++k) bstart[(size_t)h.slot_of[(size_t)to[k]] + 1]++;
     for (int32_t j = 0; j < n; ++j) bstart[j + 1] += bstart[j];
     std::vector<int64_t> order((size_t)n_syn);
     {
         std::vector<int64_t> fill(bstart.begin(), bstart.end() - 1);
-        for (int64_t k = 0; k < n_syn; ++k) order[(size_t)fill[to[k]]++] = k;
+        for (int64_t k = 0; k < n_syn; ++k) order[(size_t)fill[h.slot_of[(size_t)to[k]]]++] = k;
     }
     h.input_to_csc.assign((size_t)n_syn, -1);
     h.in_ptr.assign((size_t)n + 1, 0);
@@ -160,10 +218,10 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
             const int64_t c = (int64_t)h.csc_pre.size();
             h.input_to_csc[(size_t)k] = c;
             csc_input.push_back(k);
-            h.csc_pre.push_back(from[k]);
-            const float len = length ? length[k] : get_dist(&h.xyz[3 * (size_t)from[k]], &h.xyz[3 * (size_t)j]);
+            h.csc_pre.push_back(h.slot_of[(size_t)from[k]]);
+            const float len = length ? length[k] : get_dist(&h.xyz[3 * (size_t)from[k]], &h.xyz[3 * (size_t)to[k]]);
             const int32_t d = delay_steps(len, h.dt);
-            if (d < 0) { err = "synapse delay exceeds 32767 steps"; return NC_ERR_INVALID; }
+            if (d < 0 || d > kMaxDelay) { err = "synapse delay exceeds 16383 steps"; return NC_ERR_INVALID; }
             h.csc_delay.push_back(d);
             h.max_delay = std::max(h.max_delay, d);
             h.w.push_back(weight[k]);
@@ -205,7 +263,9 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
             const int64_t b = c - h.in_ptr[j];
             h.out_post[(size_t)q] = j;
             h.out_csc[(size_t)q] = (int32_t)c;
-            h.out_delay[(size_t)q] = (int16_t)h.csc_delay[(size_t)c];
+            // the same-step order rules compare the caller's ids of target and source
+            const uint32_t flags = (to[k] > from[k] ? 1u << kAfterBit : 0u) | (to[k] < from[k] ? 1u << kBeforeBit : 0u);
+            h.out_delay[(size_t)q] = (int16_t)(uint16_t)((uint32_t)h.csc_delay[(size_t)c] | flags);
             h.out_ringpos[(size_t)q] = ((uint32_t)(h.ring_off[j] + (int32_t)(b >> 5)) << 5) | (uint32_t)(b & 31);
         }
     }

@@ -24,7 +24,13 @@ struct NetHost {
     int32_t max_delay = 1;
     float leak = 0.5f, c52 = 0.0f;
     double e_term = 0.0;
-    std::vector<float> xyz;
+    std::vector<float> xyz;                 // caller's id order
+    std::vector<int32_t> orig_id;           // device slot -> caller's id
+    std::vector<int32_t> slot_of;           // caller's id -> device slot
+    bool permuted = false;
+    // Below, neurons are device slots.  The in-synapses of a target are sorted by the
+    // caller's source id; out_delay packs the delay (bits 0-13) and whether the target's
+    // caller id is above (bit 14) or below (bit 15) the source's.
     std::vector<int64_t> in_ptr, out_ptr;   // n+1
     std::vector<int32_t> ring_off;          // n+1
     std::vector<float> w;                   // CSC
@@ -51,6 +57,14 @@ int set_groups(NetHost& net, int32_t n_groups, const nc_group* groups, std::stri
 // Reference arithmetic helpers shared by build and read-back.
 float get_dist(const float* a, const float* b);      // coord3::getDist, src/NeuCor.h:16-18
 int32_t delay_steps(float length, float dt);          // -1 when it does not fit int16
+constexpr int32_t kMaxDelay = (1 << 14) - 1;          // delay bits of out_delay
+constexpr int kAfterBit = 14, kBeforeBit = 15;
+// Scatters a device-slot-ordered array into the caller's id order.
+template <class T>
+void to_caller_order(const NetHost& h, const T* slots, T* out)
+{
+    for (int32_t i = 0; i < h.n; ++i) out[i] = slots[h.slot_of[(size_t)i]];
+}
 uint32_t rate_threshold(float rate_hz, float dt);
 float ap_value(float x);                              // Neuron::AP, src/NeuCor.cpp:706-714
 float step_ms(int64_t k, float dt);                   // k steps as a float time difference

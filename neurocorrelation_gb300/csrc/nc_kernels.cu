@@ -52,6 +52,14 @@ __device__ __forceinline__ bool inh_bit(const NcPools& P, int64_t s)
     return (__ldg(P.inh + (s >> 5)) >> (s & 31)) & 1u;
 }
 
+// The 32 inhibitory bits of synapses s .. s+31 (s need not be word-aligned; the pool
+// keeps one spare word at its end).
+__device__ __forceinline__ uint32_t inh_bits32(const NcPools& P, int64_t s)
+{
+    const int64_t w0 = s >> 5;
+    return __funnelshift_r(__ldg(P.inh + w0), __ldg(P.inh + w0 + 1), (uint32_t)(s & 31));
+}
+
 // Synapse::synapticPlasticity weight update and clamp (src/NeuCor.cpp:757-761);
 // fmin/fmax keep the C library's generic semantics.
 __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const NcNetDesc& D)
@@ -66,6 +74,20 @@ __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, flo
         v = (m >= -1.0f) ? m : -1.0f;
     }
     return v;
+}
+
+// RN32 of a double, returned as the (exactly representable) double: the 52-bit
+// fraction is rounded to 23 bits, half to even, with integer operations.  Values
+// below the float normal range take the hardware conversion.  Together with one
+// double add this is `float += double` (src/NeuCor.cpp:695) with one FP64 operation.
+__device__ __forceinline__ double round_to_float(double d)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    if (e < 1023u - 126u) return (double)__double2float_rn(d);
+    u += 0x0FFFFFFFull + ((u >> 29) & 1ull);
+    u &= ~0x1FFFFFFFull;
+    return __longlong_as_double((long long)u);
 }
 
 __device__ __forceinline__ void philox(uint32_t a, uint32_t b, uint32_t stream, uint32_t c, const NcNetDesc& D,
@@ -99,22 +121,50 @@ __device__ bool input_request(const NcPools& P, const NcNetDesc& D, int32_t j, i
     return false;
 }
 
+// Pops up to 8 set bits of *m in ascending order into b[] (-1 when exhausted).
+__device__ __forceinline__ void pop8(uint32_t* m, int b[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        b[k] = *m ? __ffs(*m) - 1 : -1;
+        *m &= *m - 1u;
+    }
+}
+
 // Deferred plasticity of step `prev` for the 32 neurons of a tile (all lanes call).
 __device__ void tile_plasticity(const NcPools& P, const NcNetDesc& D, int64_t word, int lane, bool live,
                                 int64_t s0, int64_t s1, int32_t r0, int32_t r1, int32_t lf, int32_t prev)
 {
     const float* tab_pre = P.tables + D.table_base;
     const float* tab_post = tab_pre + D.tab_pre_len;
-    // post-spike branch: whole in-row of each neuron that fired at prev
+    // post-spike branch: the whole in-row of each neuron that fired at prev, the warp
+    // striding it four chunks at a time so the loads of a chunk group overlap
     uint32_t m = P.fired[(int64_t)(prev & 1) * P.total_words + word];
     while (m) {
         const int b = __ffs(m) - 1;
         m &= m - 1;
         const int64_t a0 = __shfl_sync(kFull, s0, b);
         const int64_t a1 = __shfl_sync(kFull, s1, b);
-        for (int64_t s = a0 + lane; s < a1; s += 32) {
-            const float trS = trace_at(tab_pre, D.tab_pre_len, prev, P.t_arr[s]);
-            P.w[s] = plasticity(P.w[s], inh_bit(P, s), trS, 0.0f, D);
+        for (int64_t base = a0; base < a1; base += 128) {
+            float wv[4];
+            int32_t ta[4];
+            bool ok[4], ih[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t s = base + lane + 32 * u;
+                ok[u] = s < a1;
+                if (ok[u]) {
+                    wv[u] = P.w[s];
+                    ta[u] = P.t_arr[s];
+                    ih[u] = inh_bit(P, s);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!ok[u]) continue;
+                const int64_t s = base + lane + 32 * u;
+                P.w[s] = plasticity(wv[u], ih[u], trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
+            }
         }
     }
     __syncwarp();
@@ -124,12 +174,22 @@ __device__ void tile_plasticity(const NcPools& P, const NcNetDesc& D, int64_t wo
         const float trT = trace_at(tab_post, D.tab_post_len, prev, lf);
         for (int32_t wi = r0; wi < r1; ++wi) {
             uint32_t bits = slot[wi];
+            if (!bits) continue;
+            const int64_t cs = s0 + (int64_t)(wi - r0) * 32;
+            const uint32_t ih = inh_bits32(P, cs);
             while (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                const int64_t s = s0 + (int64_t)(wi - r0) * 32 + b;
-                P.t_arr[s] = prev;
-                P.w[s] = plasticity(P.w[s], inh_bit(P, s), 0.0f, trT, D);
+                int b[8];
+                pop8(&bits, b);
+                float wv[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (b[k] >= 0) wv[k] = P.w[cs + b[k]];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    if (b[k] < 0) continue;
+                    P.t_arr[cs + b[k]] = prev;
+                    P.w[cs + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1u, 0.0f, trT, D);
+                }
             }
         }
     }
@@ -175,12 +235,14 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
             if (live) {
                 const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
                 bool forced = (fw >> lane) & 1u;
-                if (!forced && D.n_groups) forced = input_request(P, D, j, t);
-                // charge_insynapses (src/NeuCor.cpp:688-700)
+                if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
+                // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
+                // t-1 .. t-KC, ascending source id; the accumulator stays a float value
                 float pot = P.pot[pj];
                 if (r1 > r0) {
                     uint32_t* ring = P.ring + D.ring_base;
                     const int32_t oldest = t - D.kc;
+                    double pd = (double)pot;
                     for (int32_t wi = r0; wi < r1; ++wi) {
                         uint32_t bits = 0, last = 0;
                         for (int32_t k = 1; k <= D.kc; ++k) {
@@ -188,15 +250,22 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
                             last = ring[(int64_t)((t - k) & D.ring_mask) * D.ring_words + wi];
                             bits |= last;
                         }
+                        const double* tp = P.term + s0 + (int64_t)(wi - r0) * 32;
                         while (bits) {
-                            const int b = __ffs(bits) - 1;
-                            bits &= bits - 1;
-                            const int64_t s = s0 + (int64_t)(wi - r0) * 32 + b;
-                            pot = __double2float_rn(__dadd_rn((double)pot, P.term[s]));
+                            int b[8];
+                            pop8(&bits, b);
+                            double v[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (b[k] >= 0) v[k] = tp[b[k]];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (b[k] >= 0) pd = round_to_float(__dadd_rn(pd, v[k]));
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
                         if (oldest >= 1 && last) ring[(int64_t)(oldest & D.ring_mask) * D.ring_words + wi] = 0u;
                     }
+                    pot = __double2float_rn(pd);
                 }
                 // charge_passive (src/NeuCor.cpp:677-680)
                 pot = (pot - -70.0f) * D.leak + -70.0f;
@@ -219,12 +288,13 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
                 if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
                     D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
             }
-            // background fires for step t+1 (src/NeuCor.cpp:604-607)
+            // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
             if (live && D.bg_period > 0) {
                 uint32_t o[4];
-                philox((uint32_t)j, (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
+                philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
                 if (o[0] % (uint32_t)D.bg_period == 0u) {
-                    const uint32_t tgt = o[1] % (uint32_t)D.n;
+                    uint32_t tgt = o[1] % (uint32_t)D.n;
+                    if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
                     atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
                              1u << (tgt & 31));
                 }
@@ -295,27 +365,53 @@ __global__ void __launch_bounds__(256) k_spike_launch(NcPools P)
         const float* tab_pre = P.tables + D.table_base;
         uint32_t* ring = P.ring + D.ring_base;
         int nl = 0, nd = 0;
-        for (int64_t k = k0 + lane; k < k1; k += 32) {
-            const int32_t j = P.out_post[k];
-            const int32_t la = P.last_arr[k];
-            const int32_t need = D.kc + (j > i ? 1 : 0);
-            if (la == NC_NEVER || t - la >= need) {
-                const int64_t s = D.syn_base + P.out_csc[k];
-                float wv = P.w[s];
-                if (j < i && ((fired_t[j >> 5] >> (j & 31)) & 1u))
-                    wv = plasticity(wv, inh_bit(P, s), trace_at(tab_pre, D.tab_pre_len, t, P.t_arr[s]), 0.0f, D);
+        // four out-synapses per lane in flight: table loads, then weight loads, then writes
+        for (int64_t kb = k0; kb < k1; kb += 128) {
+            int32_t la[4], cs[4];
+            uint32_t dl[4];
+            bool ok[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t k = kb + lane + 32 * u;
+                ok[u] = k < k1;
+                if (ok[u]) {
+                    dl[u] = (uint16_t)P.out_delay[k];
+                    la[u] = P.last_arr[k];
+                    cs[u] = P.out_csc[k];
+                }
+            }
+            float wv[4];
+            bool acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                // freed by the target's update at t only if the target's id is not above
+                acc[u] = ok[u] && (la[u] == NC_NEVER || t - la[u] >= D.kc + (int32_t)((dl[u] >> 14) & 1u));
+                if (acc[u]) wv[u] = P.w[D.syn_base + cs[u]];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!ok[u]) continue;
+                if (!acc[u]) {
+                    ++nd;
+                    continue;
+                }
+                const int64_t k = kb + lane + 32 * u;
+                const int64_t s = D.syn_base + cs[u];
+                float w = wv[u];
+                if ((dl[u] >> 15) & 1u) {  // target id below the source's: its update ran first
+                    const int32_t j = P.out_post[k];
+                    if ((fired_t[j >> 5] >> (j & 31)) & 1u)
+                        w = plasticity(w, inh_bit(P, s), trace_at(tab_pre, D.tab_pre_len, t, P.t_arr[s]), 0.0f, D);
+                }
                 // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                const float depol = D.c52 * wv;
+                const float depol = D.c52 * w;
                 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT)  (src/NeuCor.cpp:695)
-                const double term = __dmul_rn(__dmul_rn((double)(D.dt * depol), 0.9943), D.e_term);
-                P.term[s] = term;
-                const int32_t d = P.out_delay[k];
+                P.term[s] = __dmul_rn(__dmul_rn((double)(D.dt * depol), 0.9943), D.e_term);
+                const int32_t d = (int32_t)(dl[u] & 0x3fffu);
                 P.last_arr[k] = t + d;
                 const uint32_t pos = P.out_ringpos[k];
                 atomicOr(ring + (int64_t)((t + d) & D.ring_mask) * D.ring_words + (pos >> 5), 1u << (pos & 31));
                 ++nl;
-            } else {
-                ++nd;
             }
         }
         nl = warp_sum(nl);
@@ -411,12 +507,13 @@ __global__ void k_mark_flushed(NcPools P)
 __global__ void k_background_prologue(NcPools P, int net)
 {
     const NcNetDesc& D = P.nets[net];
-    const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;  // caller id
     if (j >= D.n || D.bg_period <= 0) return;
     uint32_t o[4];
     philox((uint32_t)j, 0u, NC_STREAM_BACKGROUND, 0u, D, o);
     if (o[0] % (uint32_t)D.bg_period == 0u) {
-        const uint32_t tgt = o[1] % (uint32_t)D.n;
+        uint32_t tgt = o[1] % (uint32_t)D.n;
+        if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
         atomicOr(P.forced + (int64_t)(1 & 1) * P.total_words + D.word_base + (tgt >> 5), 1u << (tgt & 31));
     }
 }

@@ -139,6 +139,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         d.group_base = sl.group_base;
         d.n_groups = (int32_t)std::min<size_t>(h.groups.size(), (size_t)ngroups_each);
         d.active = 1;
+        d.permuted = h.permuted ? 1 : 0;
         d.dt = h.dt;
         d.leak = h.leak;
         d.c52 = h.c52;
@@ -169,11 +170,13 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(P.lf, int32_t, neurons);
     NC_ALLOC(P.firings, uint32_t, neurons);
     NC_ALLOC(P.act_start, int32_t, neurons);
+    NC_ALLOC(P.orig_id, int32_t, neurons);
+    NC_ALLOC(P.slot_of, int32_t, neurons);
     NC_ALLOC(P.in_ptr, int64_t, ptrs);
     NC_ALLOC(P.out_ptr, int64_t, ptrs);
     NC_ALLOC(P.ring_off, int32_t, ptrs);
     NC_ALLOC(P.w, float, syn);
-    NC_ALLOC(P.inh, uint32_t, (syn + 31) / 32);
+    NC_ALLOC(P.inh, uint32_t, (syn + 31) / 32 + 1);  // one spare word for 32-bit windows
     NC_ALLOC(P.t_arr, int32_t, syn);
     NC_ALLOC(P.term, double, syn);
     NC_ALLOC(P.out_post, int32_t, syn);
@@ -210,6 +213,8 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         std::vector<int32_t> lf((size_t)h.n, NC_NEVER);
         NC_CK(upload(P.pot, pot, sl.neuron_base, stream));
         NC_CK(upload(P.lf, lf, sl.neuron_base, stream));
+        NC_CK(upload(P.orig_id, h.orig_id, sl.neuron_base, stream));
+        NC_CK(upload(P.slot_of, h.slot_of, sl.neuron_base, stream));
         std::vector<int64_t> inp(h.in_ptr), outp(h.out_ptr);
         for (auto& v : inp) v += sl.syn_base;
         for (auto& v : outp) v += sl.syn_base;

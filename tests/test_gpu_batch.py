@@ -57,7 +57,7 @@ def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod):
     specs = mixed_nets()
     b = batch_of(nc, specs)
     shapes = [dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=0),
-              dict(neuron_block=512, launch_blocks=1216, launch_block=256, graph_steps=7),
+              dict(neuron_block=256, launch_blocks=1216, launch_block=256, graph_steps=7),
               dict(neuron_block=64, launch_blocks=3, launch_block=32, graph_steps=16)]
     done = 0
     for k, sh in enumerate(shapes * 10):
@@ -69,6 +69,15 @@ def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod):
     b.run_to_end()
     for q, s in enumerate(specs):
         check_equal(b, q, oracle_of(oracle_mod, s))
+
+
+def test_batch_rejects_oversized_blocks(nc):
+    specs = mixed_nets()[:1]
+    b = batch_of(nc, specs)
+    with pytest.raises(nc.NeuCorError):
+        b.set_launch(neuron_block=512)
+    with pytest.raises(nc.NeuCorError):
+        b.set_launch(launch_block=48)
 
 
 def test_batch_autotune_keeps_results(nc, oracle_mod):

@@ -92,6 +92,8 @@ SCENARIOS = [
     ("knn257_sign_rule", lambda: knn_net(257, 7, 25, inhibitory=0.3), dict(seed=35, inhibitory_rule=1),
      [dict(first=250, count=7, rate_hz=80.0, correlated=1, jitter=1)], 500),
     ("random64_dt4", lambda: random_net(64, 700, 26), dict(seed=36, run_speed=4.0), [], 300),
+    ("knn300_id_order", lambda: knn_net(300, 10, 28, inhibitory=0.2), dict(seed=38, storage_order=1),
+     [dict(first=40, count=20, rate_hz=30.0, correlated=1, jitter=2)], 400),
     ("knn200_nobg_lr", lambda: knn_net(200, 16, 27), dict(seed=37, background_firing=0, learning_rate=2.0,
                                                           presynaptic_factor=0.2, postsynaptic_factor=0.1),
      [dict(first=0, count=40, rate_hz=25.0, correlated=1, jitter=2)], 600),
