@@ -275,6 +275,25 @@ int nc_batch_read_potentials(nc_batch* batch, int32_t net, float* out_n);
 int nc_batch_read_weights(nc_batch* batch, int32_t net, float* out_s);
 int nc_batch_read_last_fire(nc_batch* batch, int32_t net, float* out_n);
 
+/* Advances the network like nc_run, for callers that may not allocate device memory
+ * once the network exists: code that records the step into a CUDA graph of its own
+ * (allocation is not allowed while a stream is being captured) and services running
+ * under a fixed device-memory budget.  nc_run keeps its per-step scratch (the list of
+ * neurons that fired, passed from the neuron update to the spike launch) in memory the
+ * handle allocated and replays CUDA graphs it instantiates on first use; this call
+ * launches the same two kernels directly on `stream` (NULL = the handle's own stream)
+ * and gives them a fixed scratch array compiled into the library instead, so it
+ * allocates nothing.  That array (4 MiB) is held by every GPU that loads the library
+ * until the process exits, and it limits this call to networks of at most
+ * NC_NOALLOC_MAX_NEURONS neurons; larger ones are refused with NC_ERR_INVALID.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress): make it before any
+ * stream capture.  All calls share the one array, so calls whose kernels overlap on the
+ * GPU (other handles, other streams) race: order them.  Order the call after the
+ * handle's earlier work and synchronise `stream` before reading results when it is not
+ * the handle's stream.  The reference has no counterpart: its simulator runs on the CPU. */
+#define NC_NOALLOC_MAX_NEURONS 262144
+int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream);
+
 /* Times n_steps of the handle's step kernels with CUDA events on its stream;
  * *ms receives the elapsed device time, *kernel_ms (may be NULL) two entries:
  * the mean time of one neuron-update and one spike-launch launch over a separate

@@ -5,7 +5,7 @@
 #include <string>
 #include <vector>
 
-#include "nc_pool.h"
+#include "nc_net.h"
 
 namespace {
 thread_local std::string g_err;
@@ -34,19 +34,6 @@ float render_behaviour(float val)
 }
 }  // namespace
 
-struct nc_net {
-    nc::NetHost host;
-    nc::Engine eng;
-    int64_t step = 0;      // completed steps
-    float time = 0.0f;     // NeuCor::currentTime, accumulated per step
-    uint32_t* d_raster = nullptr;
-    int32_t raster_cap = 0;
-    int32_t raster_t0 = 0;
-    ~nc_net()
-    {
-        if (d_raster) cudaFree(d_raster);
-    }
-};
 
 #define NC_NEED(net)                                                  \
     do {                                                              \

@@ -1,0 +1,70 @@
+"""nc_run_noalloc — the step for callers that may not allocate device memory once the
+network is set up (code recording the step into its own CUDA graph, where allocation is
+not allowed during stream capture; services with a fixed device-memory budget).
+
+It launches the same kernels as nc_run with their per-step scratch in a static device
+array, so it must compute exactly what nc_run computes; checked on two calls in a row,
+bit for bit (the tolerance of every parity test here), through the C ABI."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from netgen import knn_net
+
+pytestmark = pytest.mark.gpu
+
+
+def noalloc_fn(G):
+    L = G.load_library()
+    fn = L.nc_run_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+    fn.restype = ctypes.c_int32
+    return fn, L
+
+
+def make_pair(G):
+    xyz, pre, post, w = knn_net(2500, 12, 77, inhibitory=0.1)
+    groups = [dict(first=0, count=25, rate_hz=30.0, correlated=1, jitter=2),
+              dict(first=25, count=25, rate_hz=30.0, correlated=0)]
+    nets = []
+    for _ in range(2):
+        net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(seed=4242))
+        net.set_input_groups(groups)
+        nets.append(net)
+    return nets
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def test_noalloc_matches_run_on_two_calls(nc):
+    run_noalloc, L = noalloc_fn(nc)
+    ref, na = make_pair(nc)
+    for call in range(2):
+        ref.record_raster(120)
+        na.record_raster(120)
+        ref.run(120)
+        rc = run_noalloc(na._handle(), 120, None)  # NULL stream: the handle's own stream
+        assert rc == 0, L.nc_last_error().decode()
+        np.testing.assert_array_equal(na.raster(), ref.raster())
+        np.testing.assert_array_equal(bits(na.potentials()), bits(ref.potentials()))
+        np.testing.assert_array_equal(bits(na.weights()), bits(ref.weights()))
+        np.testing.assert_array_equal(bits(na.potAct), bits(ref.potAct))
+        sa, sr = na.stats(), ref.stats()
+        assert (sa["fires"], sa["launched"], sa["dropped"], sa["steps"]) == \
+            (sr["fires"], sr["launched"], sr["dropped"], sr["steps"])
+        assert sr["fires"] > 0
+        assert na.step == ref.step == 120 * (call + 1)
+
+
+def test_noalloc_refuses_networks_above_its_limit(nc):
+    run_noalloc, L = noalloc_fn(nc)
+    limit = 262144
+    xyz, pre, post, w = nc.build_knn(limit + 1, 2, 8.0, seed=3)
+    big = nc.NeuCor.from_arrays(xyz, pre, post, w)
+    rc = run_noalloc(big._handle(), 1, None)
+    assert rc == -1
+    assert str(limit) in L.nc_last_error().decode()
+    assert big.step == 0
