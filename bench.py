@@ -125,9 +125,9 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the neuron-update kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_neuron_step_c2.txt")
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary (profiles/)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_c2.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch_scaled:"):
@@ -322,7 +322,7 @@ def run_ours(args):
     alg = alg_neuron if dominant == "k_neuron_step" else alg_launch
     dur = (n_ms if dominant == "k_neuron_step" else l_ms) / 1e3
     achieved = alg / dur / 1e9
-    traffic = ncu_traffic() if dominant == "k_neuron_step" else None
+    traffic = ncu_traffic(dominant)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         port = CpuPort(arrays, groups, seed=seed, replicas=1)
