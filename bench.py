@@ -221,6 +221,116 @@ def run_reference_arm(args):
     return 0
 
 
+# ------------------------------------------------------------ batched / served
+def c3_nets(G, n_nets, horizon, seed=3):
+    """Batched workload: sizes log-uniform over 1k-64k neurons, fan-out uniform over
+    20-200 nearest neighbours, per-network seed, input rate 5-50 Hz and 1-8 correlated
+    groups of 10 input neurons."""
+    rng = np.random.default_rng(seed)
+    nets = []
+    for q in range(n_nets):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(64000))))
+        k = min(int(rng.integers(20, 201)), n - 1)
+        rate = float(rng.uniform(5.0, 50.0))
+        ng = int(rng.integers(1, 9))
+        nseed = seed * 100003 + q
+        xyz, pre, post, w = G.build_knn(n, k, 8.0, seed=nseed)
+        groups = [dict(first=10 * g, count=10, rate_hz=rate, correlated=1, jitter=2) for g in range(ng)]
+        nets.append(dict(xyz=xyz, pre=pre, post=post, weight=w, seed=nseed, groups=groups, horizon=horizon))
+    return nets
+
+
+def c4_requests(G, n_req, horizon_scale, seed=4):
+    """Served workload: Poisson arrivals at 50 requests/s; sizes log-uniform over
+    500-200k neurons, fan-out 20-150, horizons log-uniform over 1k-100k steps (times
+    horizon_scale), each with a random input pattern of 1-8 groups."""
+    rng = np.random.default_rng(seed)
+    t, reqs = 0.0, []
+    for q in range(n_req):
+        t += float(rng.exponential(1.0 / 50.0))
+        n = int(np.exp(rng.uniform(np.log(500), np.log(200000))))
+        k = min(int(rng.integers(20, 151)), n - 1)
+        h = max(1, int(np.exp(rng.uniform(np.log(1000), np.log(100000))) * horizon_scale))
+        ng = int(rng.integers(1, 9))
+        groups = [dict(first=10 * g, count=10, rate_hz=float(rng.uniform(5.0, 50.0)), correlated=int(rng.integers(0, 2)),
+                       jitter=int(rng.integers(0, 4))) for g in range(ng)]
+        nseed = seed * 100003 + q
+        xyz, pre, post, w = G.build_knn(n, k, 8.0, seed=nseed)
+        reqs.append(dict(xyz=xyz, pre=pre, post=post, weight=w, seed=nseed, groups=groups, horizon=h, arrival=t))
+    return reqs
+
+
+def one_at_a_time(G, nets, arrivals=None):
+    """The plain drop-in, one network after another: create, run the horizon, read the
+    counters, destroy.  Returns (events, busy seconds, per-request latency or None)."""
+    events, busy, clock, lat = 0, 0.0, 0.0, []
+    for q, d in enumerate(nets):
+        t0 = time.perf_counter()
+        net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"], params=G.default_params(seed=d["seed"]))
+        net.set_input_groups(d["groups"])
+        net.run(d["horizon"])
+        st = net.stats()
+        net.close()
+        dt = time.perf_counter() - t0
+        events += st["launched"]
+        busy += dt
+        if arrivals is not None:
+            start = max(arrivals[q], clock)
+            clock = start + dt
+            lat.append(clock - arrivals[q])
+    return events, busy, lat
+
+
+def measure_batched(G, n_nets, horizon):
+    nets = c3_nets(G, n_nets, horizon)
+    b = G.Batch([dict(xyz=d["xyz"], pre=d["pre"], post=d["post"], weight=d["weight"],
+                      params=G.default_params(seed=d["seed"]), groups=d["groups"], horizon=d["horizon"]) for d in nets])
+    cfg = b.autotune(steps_per_trial=4)
+    done = b.step(0)
+    before = sum(b.stats(q)["launched"] for q in range(n_nets))
+    ms = b.time(horizon - done)
+    events = sum(b.stats(q)["launched"] for q in range(n_nets)) - before
+    neurons = sum(int(d["xyz"].shape[0]) for d in nets)
+    synapses = sum(int(d["pre"].shape[0]) for d in nets)
+    b.close()
+    sub = nets[: min(len(nets), 16)]
+    ev1, busy1, _ = one_at_a_time(G, sub)
+    return {"networks": n_nets, "neurons": neurons, "synapses": synapses, "steps": horizon,
+            "timed_steps": horizon - done, "launch_config": cfg, "events_per_s": events * 1000.0 / ms,
+            "one_at_a_time_events_per_s": ev1 / busy1, "one_at_a_time_sample": len(sub),
+            "speedup_vs_one_at_a_time": (events * 1000.0 / ms) / (ev1 / busy1)}
+
+
+def measure_served(G, n_req, horizon_scale, budget):
+    reqs = c4_requests(G, n_req, horizon_scale)
+    srv = G.Server(budget, max_networks=256, steps_per_batch=64, build_threads=min(16, os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    for r in reqs:
+        wait = t0 + r["arrival"] - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        srv.submit(dict(xyz=r["xyz"], pre=r["pre"], post=r["post"], weight=r["weight"],
+                        params=G.default_params(seed=r["seed"]), groups=r["groups"], horizon=r["horizon"]))
+    srv.drain()
+    done = srv.poll()
+    sst = srv.stats()
+    srv.close()
+    ok = [d for d in done if d["status"] == 0]
+    lat = np.array([d["done_s"] - d["submit_s"] for d in ok])
+    span = max(d["done_s"] for d in ok) - min(d["submit_s"] for d in ok)
+    events = sum(d["launched"] for d in ok)
+    ev1, busy1, lat1 = one_at_a_time(G, reqs, arrivals=[r["arrival"] for r in reqs])
+    span1 = max(a + l for a, l in zip([r["arrival"] for r in reqs], lat1)) - reqs[0]["arrival"]
+    return {"requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
+            "budget_gb": budget / 1e9, "events_per_s": events / span, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "peak_resident_networks": sst["peak_resident_networks"],
+            "peak_resident_gb": sst["peak_resident_bytes"] / 1e9,
+            "one_at_a_time_events_per_s": ev1 / span1,
+            "one_at_a_time_p50_latency_s": float(np.percentile(lat1, 50)),
+            "one_at_a_time_p99_latency_s": float(np.percentile(lat1, 99)),
+            "speedup_vs_one_at_a_time": (events / span) / (ev1 / span1)}
+
+
 def run_ours(args):
     world, rank, local = dist_env()
     pg = None
@@ -346,6 +456,10 @@ def run_ours(args):
         "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
     }
+    if world == 1 and args.forms:
+        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps),
+                         "served": measure_served(G, args.served_requests, args.served_horizon_scale,
+                                                  args.served_budget_gb * 1e9)}
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
@@ -360,6 +474,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-forms", dest="forms", action="store_false",
+                    help="skip the batched and served samples")
+    ap.add_argument("--batched-nets", type=int, default=64)
+    ap.add_argument("--batched-steps", type=int, default=2000)
+    ap.add_argument("--served-requests", type=int, default=32)
+    ap.add_argument("--served-horizon-scale", type=float, default=0.1)
+    ap.add_argument("--served-budget-gb", type=float, default=120.0)
     ap.add_argument("--sim-steps-per-step", type=int, default=SIM_STEPS_PER_STEP,
                     help="simulation steps per bench step (smaller values make ncu-sized cases)")
     args = ap.parse_args()

@@ -275,6 +275,60 @@ int nc_batch_read_potentials(nc_batch* batch, int32_t net, float* out_n);
 int nc_batch_read_weights(nc_batch* batch, int32_t net, float* out_s);
 int nc_batch_read_last_fire(nc_batch* batch, int32_t net, float* out_n);
 
+/* ---------------------------------------------------------- served form */
+/* A request server: simulation jobs (networks with their own size, inputs and
+ * horizon) are submitted while others run; each is admitted when its device
+ * footprint fits the memory budget and a slot is free, stays resident on the device
+ * while it runs, and leaves when it reaches its horizon.  Networks admitted at
+ * different times advance together in the same launches (continuous batching); each
+ * computes the same bits it would alone.  No reference counterpart: the reference
+ * simulates one NeuCor at a time. */
+typedef struct nc_server nc_server;
+
+typedef struct {
+    int64_t memory_budget_bytes; /* device memory for resident networks */
+    int32_t max_networks;        /* networks resident at once */
+    int32_t steps_per_batch;     /* steps between admission / completion decisions */
+    int32_t build_threads;       /* host threads preparing submitted networks */
+    int32_t keep_results;        /* 1: keep finished networks' weights and potentials for nc_server_fetch */
+} nc_server_config;
+
+typedef struct {
+    int64_t request_id;
+    int32_t status;    /* NC_OK, or why the request was refused (NC_ERR_BUDGET, NC_ERR_INVALID) */
+    int32_t n_neurons;
+    int32_t horizon;
+    int32_t reserved;
+    int64_t n_synapses;
+    double submit_s;   /* seconds since the server started */
+    double admit_s;
+    double done_s;
+    nc_stats stats;
+} nc_request_done;
+
+typedef struct {
+    int64_t submitted, admitted, finished, rejected;
+    int64_t resident_bytes;      /* footprint of the networks resident now */
+    int64_t peak_resident_bytes;
+    int64_t peak_resident_networks;
+    int64_t steps_run;           /* launch pairs issued */
+    double device_busy_s;        /* device time of the step batches */
+} nc_server_stats;
+
+int nc_server_create(const nc_server_config* config, nc_server** out);
+/* Copies the spec's arrays; returns at once.  NC_ERR_BUDGET if the network could never
+ * fit the budget. */
+int nc_server_submit(nc_server* server, const nc_net_spec* spec, int64_t* request_id);
+/* Finished requests since the last poll (at most `capacity`). */
+int nc_server_poll(nc_server* server, nc_request_done* out, int32_t capacity, int32_t* count);
+/* Blocks until every submitted request has finished. */
+int nc_server_drain(nc_server* server);
+/* Final weights (creation order, as nc_read_weights) and potentials of a finished
+ * request, when the server keeps results; either pointer may be NULL.  Releases them. */
+int nc_server_fetch(nc_server* server, int64_t request_id, float* weights, float* potentials);
+int nc_server_get_stats(nc_server* server, nc_server_stats* out);
+int nc_server_destroy(nc_server* server);
+
 /* Advances the network like nc_run, for callers that may not allocate device memory
  * once the network exists: code that records the step into a CUDA graph of its own
  * (allocation is not allowed while a stream is being captured) and services running

@@ -122,6 +122,10 @@ def load_library() -> ctypes.CDLL:
         "nc_batch_autotune": ([P, I32, P], I32), "nc_batch_get_stats": ([P, I32, P], I32),
         "nc_batch_get_step": ([P, I32, P], I32), "nc_batch_read_potentials": ([P, I32, P], I32),
         "nc_batch_read_weights": ([P, I32, P], I32), "nc_batch_read_last_fire": ([P, I32, P], I32),
+        "nc_server_create": ([P, P], I32), "nc_server_submit": ([P, P, P], I32),
+        "nc_server_poll": ([P, P, I32, P], I32), "nc_server_drain": ([P], I32),
+        "nc_server_fetch": ([P, I64, P, P], I32), "nc_server_get_stats": ([P, P], I32),
+        "nc_server_destroy": ([P], I32), "nc_run_noalloc": ([P, I32, P], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -613,3 +617,93 @@ class Batch:
         out = np.zeros(self.sizes[net], dtype=np.float32)
         _check(self._lib.nc_batch_read_last_fire(self._h, int(net), _p(out)))
         return out
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_int64), ("max_networks", ctypes.c_int32),
+                ("steps_per_batch", ctypes.c_int32), ("build_threads", ctypes.c_int32),
+                ("keep_results", ctypes.c_int32)]
+
+
+class RequestDone(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_int64), ("status", ctypes.c_int32), ("n_neurons", ctypes.c_int32),
+                ("horizon", ctypes.c_int32), ("reserved", ctypes.c_int32), ("n_synapses", ctypes.c_int64),
+                ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("stats", _Stats)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "stats"}
+        d.update({f: int(getattr(self.stats, f)) for f, _ in _Stats._fields_})
+        return d
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("finished", ctypes.c_int64),
+                ("rejected", ctypes.c_int64), ("resident_bytes", ctypes.c_int64),
+                ("peak_resident_bytes", ctypes.c_int64), ("peak_resident_networks", ctypes.c_int64),
+                ("steps_run", ctypes.c_int64), ("device_busy_s", ctypes.c_double)]
+
+
+class Server:
+    """Request server (nc_server_*): networks submitted while others run are admitted by
+    device footprint, advance together in shared launches and leave at their horizon."""
+
+    def __init__(self, budget_bytes: int, max_networks: int = 256, steps_per_batch: int = 64,
+                 build_threads: int = 8, keep_results: bool = False):
+        self._lib = load_library()
+        cfg = ServerConfig(int(budget_bytes), int(max_networks), int(steps_per_batch), int(build_threads),
+                           int(bool(keep_results)))
+        h = ctypes.c_void_p()
+        _check(self._lib.nc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.sizes = {}
+
+    def submit(self, d) -> int:
+        xyz = np.ascontiguousarray(d["xyz"], dtype=np.float32).reshape(-1, 3)
+        pre = np.ascontiguousarray(d["pre"], dtype=np.int32)
+        post = np.ascontiguousarray(d["post"], dtype=np.int32)
+        w = np.ascontiguousarray(d["weight"], dtype=np.float32)
+        groups = d.get("groups", [])
+        garr = (Group * max(1, len(groups)))()
+        for i, g in enumerate(groups):
+            garr[i] = Group(int(g["first"]), int(g["count"]), float(g["rate_hz"]), int(g.get("correlated", 1)),
+                            int(g.get("jitter", 2)))
+        spec = NetSpec(xyz.shape[0], _p(xyz), pre.shape[0], _p(pre), _p(post), _p(w), None, None,
+                       d.get("params") or default_params(), len(groups), ctypes.cast(garr, ctypes.c_void_p),
+                       int(d["horizon"]))
+        rid = ctypes.c_int64()
+        _check(self._lib.nc_server_submit(self._h, ctypes.byref(spec), ctypes.byref(rid)))
+        self.sizes[rid.value] = (xyz.shape[0], pre.shape[0])
+        return int(rid.value)
+
+    def poll(self, capacity: int = 4096):
+        arr = (RequestDone * capacity)()
+        n = ctypes.c_int32()
+        _check(self._lib.nc_server_poll(self._h, ctypes.cast(arr, ctypes.c_void_p), capacity, ctypes.byref(n)))
+        return [arr[i].as_dict() for i in range(n.value)]
+
+    def drain(self):
+        _check(self._lib.nc_server_drain(self._h))
+
+    def fetch(self, rid: int):
+        n, s = self.sizes[rid]
+        w = np.zeros(s, dtype=np.float32)
+        pot = np.zeros(n, dtype=np.float32)
+        _check(self._lib.nc_server_fetch(self._h, int(rid), _p(w), _p(pot)))
+        return w, pot
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self._lib.nc_server_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -234,12 +234,18 @@ int nc_record_raster(nc_net* net, int32_t max_steps)
     if (net->d_raster && max_steps != net->raster_cap) {
         cudaFree(net->d_raster);
         net->d_raster = nullptr;
+        if (net->d_raster_ids) cudaFree(net->d_raster_ids);
+        net->d_raster_ids = nullptr;
         net->raster_cap = 0;
     }
     if (max_steps > 0 && !net->d_raster) {
         const size_t words = (size_t)max_steps * net->eng.slots[0].n_words;
         cudaError_t e = cudaMalloc(&net->d_raster, std::max<size_t>(words, 1) * sizeof(uint32_t));
         if (e != cudaSuccess) return fail(NC_ERR_NOMEM, nc::cuda_msg("cudaMalloc raster", e));
+        if (net->host.permuted) {
+            e = cudaMalloc(&net->d_raster_ids, std::max<size_t>(words, 1) * sizeof(uint32_t));
+            if (e != cudaSuccess) return fail(NC_ERR_NOMEM, nc::cuda_msg("cudaMalloc raster", e));
+        }
         e = cudaMemset(net->d_raster, 0, std::max<size_t>(words, 1) * sizeof(uint32_t));
         if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("cudaMemset raster", e));
         net->raster_cap = max_steps;
@@ -259,23 +265,19 @@ int nc_read_raster(nc_net* net, uint8_t* out, int64_t capacity_bytes, int32_t* s
     *steps = rows;
     if (!out) return NC_OK;
     if (capacity_bytes < rows * row_bytes) return fail(NC_ERR_INVALID, "raster buffer too small");
-    std::vector<uint32_t> buf((size_t)rows * nw);
-    NC_CALL(net->eng, download, buf.data(), (const uint32_t*)net->d_raster, buf.size());
     const nc::NetHost& h = net->host;
-    for (int32_t r = 0; r < rows; ++r) {
-        uint8_t* o = out + (int64_t)r * row_bytes;
-        const uint32_t* b = buf.data() + (size_t)r * nw;
-        if (!h.permuted) {
-            std::memcpy(o, b, (size_t)row_bytes);
-            continue;
-        }
-        std::memset(o, 0, (size_t)row_bytes);
-        for (int32_t s = 0; s < h.n; ++s)
-            if ((b[s >> 5] >> (s & 31)) & 1u) {
-                const int32_t i = h.orig_id[(size_t)s];
-                o[i >> 3] |= (uint8_t)(1u << (i & 7));
-            }
+    const uint32_t* src = net->d_raster;
+    if (h.permuted && rows > 0) {
+        const auto& sl = net->eng.slots[0];
+        if (nc::launch_raster_to_ids(net->d_raster, net->d_raster_ids, net->eng.P.slot_of + sl.neuron_base, h.n, nw,
+                                     rows, net->eng.stream))
+            return fail(NC_ERR_CUDA, nc::cuda_msg("raster reorder", cudaGetLastError()));
+        src = net->d_raster_ids;
     }
+    std::vector<uint32_t> buf((size_t)rows * nw);
+    NC_CALL(net->eng, download, buf.data(), src, buf.size());
+    for (int32_t r = 0; r < rows; ++r)
+        std::memcpy(out + (int64_t)r * row_bytes, buf.data() + (size_t)r * nw, (size_t)row_bytes);
     return NC_OK;
 }
 

@@ -128,6 +128,7 @@ struct NcPools {
     int32_t n_nets;
     NcTile* tiles;
     int32_t n_tiles;
+    int32_t* n_tiles_dev; // when set, the tile count is read from device memory (served engine)
     // engine
     int32_t* tick;       // engine tick (parity of the fired list)
     uint32_t* done_ctr;  // last-block detection
@@ -178,4 +179,6 @@ int launch_spike_launch(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_stdp_flush(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);
+int launch_raster_to_ids(const uint32_t* in, uint32_t* out, const int32_t* slot_of, int32_t n, int32_t n_words,
+                         int32_t rows, void* stream);
 }  // namespace nc

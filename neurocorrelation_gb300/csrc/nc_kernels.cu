@@ -201,12 +201,17 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
     __shared__ int s_base;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int wpb = blockDim.x >> 5;
     const int tick = *P.tick;
+    const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
 
+    // blocks stride over the tile table (block-uniform loop: the compaction barriers
+    // below are reached by every thread)
+    for (int base = blockIdx.x * wpb; base < n_tiles; base += gridDim.x * wpb) {
+    const int gw = base + wib;
     uint32_t fmask = 0;
     int net = 0, first = 0;
-    if (gw < P.n_tiles) {
+    if (gw < n_tiles) {
         const NcTile tile = P.tiles[gw];
         const NcNetDesc& D = P.nets[tile.net];
         const int32_t t = D.t;
@@ -318,6 +323,8 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
     if ((fmask >> lane) & 1u) {
         const int rank = __popc(fmask & ((1u << lane) - 1u));
         P.fired_list[(int64_t)(tick & 1) * P.fired_cap + s_base + s_cnt[wib] + rank] = make_int2(net, first + lane);
+    }
+    __syncthreads();  // s_cnt and s_base are reused by the next tile group
     }
 }
 
@@ -528,9 +535,38 @@ __global__ void k_force_bits(NcPools P, int net, const int32_t* ids, int count)
     atomicOr(P.forced + (int64_t)(D.t & 1) * P.total_words + D.word_base + (j >> 5), 1u << (j & 31));
 }
 
+// Raster rows from device-slot order to caller-id order: thread per output word.
+__global__ void k_raster_to_ids(const uint32_t* in, uint32_t* out, const int32_t* slot_of, int32_t n, int32_t n_words,
+                                int32_t rows)
+{
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (int64_t)rows * n_words) return;
+    const int32_t r = (int32_t)(q / n_words), w = (int32_t)(q % n_words);
+    const uint32_t* row = in + (int64_t)r * n_words;
+    uint32_t v = 0;
+    for (int b = 0; b < 32; ++b) {
+        const int32_t i = w * 32 + b;
+        if (i >= n) break;
+        const int32_t s = __ldg(slot_of + i);
+        v |= ((__ldg(row + (s >> 5)) >> (s & 31)) & 1u) << b;
+    }
+    out[q] = v;
+}
+
 }  // namespace
 
 namespace nc {
+
+int launch_raster_to_ids(const uint32_t* in, uint32_t* out, const int32_t* slot_of, int32_t n, int32_t n_words,
+                         int32_t rows, void* stream)
+{
+    const int64_t total = (int64_t)rows * n_words;
+    if (total <= 0) return 0;
+    k_raster_to_ids<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in, out, slot_of, n, n_words,
+                                                                                       rows);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 
 static int check_launch()
 {
