@@ -34,6 +34,7 @@ SIM_STEPS_PER_STEP = 1000
 N_GROUPS, GROUP_SIZE = 10, 20
 METRIC = "synaptic events/s"
 UNIT = "events/s"
+STEP_MODES = {"dense": 0, "event": 1}
 
 
 def workload_groups():
@@ -260,13 +261,14 @@ def c4_requests(G, n_req, horizon_scale, seed=4):
     return reqs
 
 
-def one_at_a_time(G, nets, arrivals=None):
+def one_at_a_time(G, nets, mode, arrivals=None):
     """The plain drop-in, one network after another: create, run the horizon, read the
     counters, destroy.  Returns (events, busy seconds, per-request latency or None)."""
     events, busy, clock, lat = 0, 0.0, 0.0, []
     for q, d in enumerate(nets):
         t0 = time.perf_counter()
-        net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"], params=G.default_params(seed=d["seed"]))
+        net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"],
+                                   params=G.default_params(seed=d["seed"], step_mode=mode))
         net.set_input_groups(d["groups"])
         net.run(d["horizon"])
         st = net.stats()
@@ -281,10 +283,11 @@ def one_at_a_time(G, nets, arrivals=None):
     return events, busy, lat
 
 
-def measure_batched(G, n_nets, horizon):
+def measure_batched(G, n_nets, horizon, mode):
     nets = c3_nets(G, n_nets, horizon)
     b = G.Batch([dict(xyz=d["xyz"], pre=d["pre"], post=d["post"], weight=d["weight"],
-                      params=G.default_params(seed=d["seed"]), groups=d["groups"], horizon=d["horizon"]) for d in nets])
+                      params=G.default_params(seed=d["seed"], step_mode=mode), groups=d["groups"],
+                      horizon=d["horizon"]) for d in nets])
     cfg = b.autotune(steps_per_trial=4)
     done = b.step(0)
     before = sum(b.stats(q)["launched"] for q in range(n_nets))
@@ -294,23 +297,25 @@ def measure_batched(G, n_nets, horizon):
     synapses = sum(int(d["pre"].shape[0]) for d in nets)
     b.close()
     sub = nets[: min(len(nets), 16)]
-    ev1, busy1, _ = one_at_a_time(G, sub)
+    ev1, busy1, _ = one_at_a_time(G, sub, mode)
     return {"networks": n_nets, "neurons": neurons, "synapses": synapses, "steps": horizon,
             "timed_steps": horizon - done, "launch_config": cfg, "events_per_s": events * 1000.0 / ms,
             "one_at_a_time_events_per_s": ev1 / busy1, "one_at_a_time_sample": len(sub),
             "speedup_vs_one_at_a_time": (events * 1000.0 / ms) / (ev1 / busy1)}
 
 
-def measure_served(G, n_req, horizon_scale, budget):
+def measure_served(G, n_req, horizon_scale, budget, mode):
     reqs = c4_requests(G, n_req, horizon_scale)
-    srv = G.Server(budget, max_networks=256, steps_per_batch=64, build_threads=min(16, os.cpu_count() or 1))
+    srv = G.Server(budget, max_networks=256, steps_per_batch=64, build_threads=min(16, os.cpu_count() or 1),
+                   step_mode=mode)
     t0 = time.perf_counter()
     for r in reqs:
         wait = t0 + r["arrival"] - time.perf_counter()
         if wait > 0:
             time.sleep(wait)
         srv.submit(dict(xyz=r["xyz"], pre=r["pre"], post=r["post"], weight=r["weight"],
-                        params=G.default_params(seed=r["seed"]), groups=r["groups"], horizon=r["horizon"]))
+                        params=G.default_params(seed=r["seed"], step_mode=mode), groups=r["groups"],
+                        horizon=r["horizon"]))
     srv.drain()
     done = srv.poll()
     sst = srv.stats()
@@ -319,7 +324,7 @@ def measure_served(G, n_req, horizon_scale, budget):
     lat = np.array([d["done_s"] - d["submit_s"] for d in ok])
     span = max(d["done_s"] for d in ok) - min(d["submit_s"] for d in ok)
     events = sum(d["launched"] for d in ok)
-    ev1, busy1, lat1 = one_at_a_time(G, reqs, arrivals=[r["arrival"] for r in reqs])
+    ev1, busy1, lat1 = one_at_a_time(G, reqs, mode, arrivals=[r["arrival"] for r in reqs])
     span1 = max(a + l for a, l in zip([r["arrival"] for r in reqs], lat1)) - reqs[0]["arrival"]
     return {"requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
             "budget_gb": budget / 1e9, "events_per_s": events / span, "p50_latency_s": float(np.percentile(lat, 50)),
@@ -351,7 +356,8 @@ def run_ours(args):
     groups = workload_groups()
     seed = 1 + rank
     arrays = build_network(G, seed=seed)
-    net = G.NeuCor.from_arrays(*arrays, params=G.default_params(seed=seed))
+    mode = STEP_MODES[args.step_mode]
+    net = G.NeuCor.from_arrays(*arrays, params=G.default_params(seed=seed, step_mode=mode))
     net.set_input_groups(groups)
     S = SIM_STEPS_PER_STEP
 
@@ -423,14 +429,20 @@ def run_ours(args):
     neuron_steps = N_NEURONS * args.steps * S * world / secs
     peak, peak_kind = measured_peak()
     n_ms, l_ms = per
-    dominant = "k_neuron_step" if n_ms >= l_ms else "k_spike_launch"
-    # algorithmic bytes (16 per neuron + 14 per synaptic event per step): the neuron
-    # update moves 16 per neuron and 8 per event (weight read+write of plasticity), the
-    # spike launch 6 per event (target index 4 + delay 2)
-    alg_neuron = 16.0 * N_NEURONS + 8.0 * ev_per_step_k
-    alg_launch = 6.0 * ev_per_step_k
-    alg = alg_neuron if dominant == "k_neuron_step" else alg_launch
-    dur = (n_ms if dominant == "k_neuron_step" else l_ms) / 1e3
+    if args.step_mode == "dense":
+        # the synapse pass moves the 14 bytes per synaptic event (index 4, delay 2,
+        # weight read + write 8), the neuron pass the 16 per neuron
+        kernels = {"k_dense_synapses": n_ms, "k_dense_neurons": l_ms}
+        dominant = "k_dense_synapses" if n_ms >= l_ms else "k_dense_neurons"
+        alg = 14.0 * ev_per_step_k if dominant == "k_dense_synapses" else 16.0 * N_NEURONS
+    else:
+        kernels = {"k_neuron_step": n_ms, "k_spike_launch": l_ms}
+        dominant = "k_neuron_step" if n_ms >= l_ms else "k_spike_launch"
+        # algorithmic bytes (16 per neuron + 14 per synaptic event per step): the neuron
+        # update moves 16 per neuron and 8 per event (weight read+write of plasticity),
+        # the spike launch 6 per event (target index 4 + delay 2)
+        alg = 16.0 * N_NEURONS + 8.0 * ev_per_step_k if dominant == "k_neuron_step" else 6.0 * ev_per_step_k
+    dur = kernels[dominant] / 1e3
     achieved = alg / dur / 1e9
     traffic = ncu_traffic(dominant)
     cpu = None
@@ -444,22 +456,23 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config({"neuron_steps_per_s": neuron_steps, "spikes_per_s": fires * world / secs,
+        "config": workload_config({"step_mode": args.step_mode, "neuron_steps_per_s": neuron_steps,
+                                   "spikes_per_s": fires * world / secs,
                                    "mean_rate_hz": fires / (N_NEURONS * args.steps * S / 1000.0),
                                    "step_pair_alg_gbs": step_alg}),
-        "gpu_launches": 2 * args.steps * S,
+        "gpu_launches": (1 if args.step_mode == "dense" else 2) * args.steps * S,
         "clocks": clk.summary(),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "neuron_step_ms": n_ms, "spike_launch_ms": l_ms,
+                     "kernel_ms": kernels,
                      "events_per_step_in_kernel_pass": ev_per_step_k},
         "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
     }
     if world == 1 and args.forms:
-        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps),
+        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, mode),
                          "served": measure_served(G, args.served_requests, args.served_horizon_scale,
-                                                  args.served_budget_gb * 1e9)}
+                                                  args.served_budget_gb * 1e9, mode)}
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
@@ -473,6 +486,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--step-mode", default="dense", choices=sorted(STEP_MODES),
+                    help="form of the step kernels (results are the same in both)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the batched and served samples")

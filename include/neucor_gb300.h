@@ -65,7 +65,7 @@ typedef struct {
     int32_t inhibitory_rule;        /* NC_INHIBITORY_* below */
     uint64_t seed;                  /* key of the counter-based draws (background, inputs) */
     int32_t storage_order;          /* NC_ORDER_*: how neurons are laid out in device memory */
-    int32_t reserved;
+    int32_t step_mode;              /* NC_STEP_*: which form of the step kernels runs */
 } nc_params;
 
 /* Device layout of neurons.  Results never depend on it (ids, the in-synapse fold
@@ -76,6 +76,18 @@ typedef struct {
  *   NC_ORDER_ID       the caller's id order. */
 #define NC_ORDER_SPATIAL 0
 #define NC_ORDER_ID 1
+
+/* Form of the step kernels.  Results never depend on it.
+ *   NC_STEP_DENSE  (default) one launch per step; each warp walks its 32 targets'
+ *                  in-synapse rows in order, making the launch decisions, the plasticity
+ *                  and the arrival window there.  Its cost grows with the synapse count:
+ *                  the faster form when a large share of neurons fires every step.
+ *   NC_STEP_EVENT  two launches per step; fired neurons are compacted into a list and
+ *                  only their out-synapses and the arrived spikes are touched.  Its cost
+ *                  grows with the synaptic events: the faster form for sparse activity.
+ * Networks batched into one engine (nc_batch_create) run in the first network's form. */
+#define NC_STEP_DENSE 0
+#define NC_STEP_EVENT 1
 
 /* A group of input neurons driven by Poisson spike trains.  Members are the
  * neurons first .. first+count-1.  Correlated groups share one source whose every
@@ -249,10 +261,12 @@ typedef struct {
 
 /* Launch configuration of an engine (the autotuner's search space). */
 typedef struct {
-    int32_t neuron_block;        /* threads per block of the neuron update (32..256, multiple of 32) */
-    int32_t launch_blocks;       /* blocks of the spike launch */
-    int32_t launch_block;        /* threads per block of the spike launch (32..256, multiple of 32) */
-    int32_t graph_steps;         /* launch pairs per captured CUDA graph */
+    int32_t neuron_block;        /* threads per block of the neuron update, or of the dense step
+                                    (32..256, multiple of 32) */
+    int32_t launch_blocks;       /* event form: blocks of the spike launch */
+    int32_t launch_block;        /* event form: threads per block of the spike launch (32..256) */
+    int32_t graph_steps;         /* steps per captured CUDA graph */
+    int32_t dense_blocks;        /* dense form: blocks of the step launch; 0 = one warp per 32 neurons */
 } nc_launch_config;
 
 int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out);
@@ -291,6 +305,7 @@ typedef struct {
     int32_t steps_per_batch;     /* steps between admission / completion decisions */
     int32_t build_threads;       /* host threads preparing submitted networks */
     int32_t keep_results;        /* 1: keep finished networks' weights and potentials for nc_server_fetch */
+    int32_t step_mode;           /* NC_STEP_*: form of the step kernels for every request */
 } nc_server_config;
 
 typedef struct {
@@ -332,26 +347,29 @@ int nc_server_destroy(nc_server* server);
 /* Advances the network like nc_run, for callers that may not allocate device memory
  * once the network exists: code that records the step into a CUDA graph of its own
  * (allocation is not allowed while a stream is being captured) and services running
- * under a fixed device-memory budget.  nc_run keeps its per-step scratch (the list of
- * neurons that fired, passed from the neuron update to the spike launch) in memory the
- * handle allocated and replays CUDA graphs it instantiates on first use; this call
- * launches the same two kernels directly on `stream` (NULL = the handle's own stream)
- * and gives them a fixed scratch array compiled into the library instead, so it
+ * under a fixed device-memory budget.  nc_run replays CUDA graphs it instantiates on
+ * first use and, in the event form (NC_STEP_EVENT), keeps its per-step scratch (the
+ * list of neurons that fired, passed from the neuron update to the spike launch) in
+ * memory the handle allocated.  This call launches the same kernels directly on
+ * `stream` (NULL = the handle's own stream).  The dense form needs no scratch; the
+ * event form gets a fixed scratch array compiled into the library instead, so the call
  * allocates nothing.  That array (4 MiB) is held by every GPU that loads the library
- * until the process exits, and it limits this call to networks of at most
+ * until the process exits, and it limits event-form calls to networks of at most
  * NC_NOALLOC_MAX_NEURONS neurons; larger ones are refused with NC_ERR_INVALID.  The
- * first call on a device looks the array up (cudaGetSymbolAddress): make it before any
- * stream capture.  All calls share the one array, so calls whose kernels overlap on the
- * GPU (other handles, other streams) race: order them.  Order the call after the
- * handle's earlier work and synchronise `stream` before reading results when it is not
- * the handle's stream.  The reference has no counterpart: its simulator runs on the CPU. */
+ * first event-form call on a device looks the array up (cudaGetSymbolAddress): make it
+ * before any stream capture.  All event-form calls share the one array, so calls whose
+ * kernels overlap on the GPU (other handles, other streams) race: order them.  Order
+ * the call after the handle's earlier work and synchronise `stream` before reading
+ * results when it is not the handle's stream.  The reference has no counterpart: its
+ * simulator runs on the CPU. */
 #define NC_NOALLOC_MAX_NEURONS 262144
 int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream);
 
 /* Times n_steps of the handle's step kernels with CUDA events on its stream;
  * *ms receives the elapsed device time, *kernel_ms (may be NULL) two entries:
  * the mean time of one neuron-update and one spike-launch launch over a separate
- * instrumented pass of min(n_steps, 200) steps. */
+ * instrumented pass of min(n_steps, 200) steps (dense form: the synapse pass and the
+ * neuron pass). */
 int nc_time_steps(nc_net* net, int32_t n_steps, float* ms, float* kernel_ms);
 
 #ifdef __cplusplus

@@ -23,6 +23,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_lib", "libneucor_gb300.so")
 
 NC_OK = 0
+NC_STEP_DENSE = 0  # step_mode: one launch per step, in-rows walked in order
+NC_STEP_EVENT = 1  # step_mode: fired-list compaction and spike launch (sparse activity)
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "no CUDA device",
            -6: "device wait timed out", -7: "over memory budget"}
 
@@ -46,7 +48,7 @@ class Params(ctypes.Structure):
         ("inhibitory_rule", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
         ("storage_order", ctypes.c_int32),
-        ("reserved2", ctypes.c_int32),
+        ("step_mode", ctypes.c_int32),
     ]
 
 
@@ -74,7 +76,7 @@ class NetSpec(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("neuron_block", ctypes.c_int32), ("launch_blocks", ctypes.c_int32), ("launch_block", ctypes.c_int32),
-                ("graph_steps", ctypes.c_int32)]
+                ("graph_steps", ctypes.c_int32), ("dense_blocks", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}
@@ -622,7 +624,7 @@ class Batch:
 class ServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget_bytes", ctypes.c_int64), ("max_networks", ctypes.c_int32),
                 ("steps_per_batch", ctypes.c_int32), ("build_threads", ctypes.c_int32),
-                ("keep_results", ctypes.c_int32)]
+                ("keep_results", ctypes.c_int32), ("step_mode", ctypes.c_int32)]
 
 
 class RequestDone(ctypes.Structure):
@@ -649,10 +651,10 @@ class Server:
     device footprint, advance together in shared launches and leave at their horizon."""
 
     def __init__(self, budget_bytes: int, max_networks: int = 256, steps_per_batch: int = 64,
-                 build_threads: int = 8, keep_results: bool = False):
+                 build_threads: int = 8, keep_results: bool = False, step_mode: int = 0):
         self._lib = load_library()
         cfg = ServerConfig(int(budget_bytes), int(max_networks), int(steps_per_batch), int(build_threads),
-                           int(bool(keep_results)))
+                           int(bool(keep_results)), int(step_mode))
         h = ctypes.c_void_p()
         _check(self._lib.nc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -122,12 +122,12 @@ int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int
         delete net;
         return fail(rc, err);
     }
-    // keep on the host only what read-back needs
+    // keep on the host only what read-back needs (the out-synapse tables serve the
+    // synapse snapshots)
     nc::NetHost& h = net->host;
-    std::vector<int32_t>().swap(h.out_post);
-    std::vector<int32_t>().swap(h.out_csc);
-    std::vector<int16_t>().swap(h.out_delay);
     std::vector<uint32_t>().swap(h.out_ringpos);
+    std::vector<int32_t>().swap(h.csc_pre);
+    std::vector<uint16_t>().swap(h.csc_dl);
     std::vector<float>().swap(h.w);
     std::vector<int64_t>().swap(h.in_ptr);
     std::vector<int32_t>().swap(h.ring_off);
@@ -394,33 +394,29 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
     const auto& sl = net->eng.slots[0];
     const auto& P = net->eng.P;
     std::vector<float> w((size_t)h.s);
-    std::vector<int32_t> post((size_t)h.s), csc((size_t)h.s), la((size_t)h.s);
-    std::vector<int16_t> dly((size_t)h.s);
-    std::vector<int64_t> optr((size_t)h.n + 1);
+    std::vector<int32_t> la((size_t)h.s);  // CSC order (dense form) or out-synapse order (event form)
     NC_CALL(net->eng, download, w.data(), (const float*)P.w + sl.syn_base, (size_t)h.s);
-    NC_CALL(net->eng, download, post.data(), (const int32_t*)P.out_post + sl.syn_base, (size_t)h.s);
-    NC_CALL(net->eng, download, csc.data(), (const int32_t*)P.out_csc + sl.syn_base, (size_t)h.s);
-    NC_CALL(net->eng, download, la.data(), (const int32_t*)P.last_arr + sl.syn_base, (size_t)h.s);
-    NC_CALL(net->eng, download, dly.data(), (const int16_t*)P.out_delay + sl.syn_base, (size_t)h.s);
-    NC_CALL(net->eng, download, optr.data(), (const int64_t*)P.out_ptr + sl.ptr_base, (size_t)h.n + 1);
+    const bool dense = net->eng.dense;
+    NC_CALL(net->eng, download, la.data(), (const int32_t*)(dense ? P.la_c : P.last_arr) + sl.syn_base, (size_t)h.s);
     const float T = net->time;
     const int64_t t = net->step;
     int64_t q = 0;
     for (int32_t i = 0; i < h.n; ++i) {
         const int32_t si = h.slot_of[(size_t)i];
-        for (int64_t k = optr[si] - sl.syn_base; k < optr[si + 1] - sl.syn_base; ++k) {
+        for (int64_t k = h.out_ptr[(size_t)si]; k < h.out_ptr[(size_t)si + 1]; ++k) {
             nc_synapse_snapshot& o = out[q++];
-            const float weight = w[(size_t)csc[(size_t)k]];
+            const int32_t c = h.out_csc[(size_t)k];
+            const float weight = w[(size_t)c];
             o.from_id = i;
-            o.to_id = h.orig_id[(size_t)post[(size_t)k]];
+            o.to_id = h.orig_id[(size_t)h.out_post[(size_t)k]];
             o.weight = weight;
             o.inhibitory = weight < 0.0f;
             o.pre_potential = 0.0f;
             o.post_potential = 0.0f;
-            const int32_t a = la[(size_t)k];
+            const int32_t a = la[(size_t)(dense ? c : k)];
             // in flight (AP_fireTime != 0) until its target's update KC steps after arrival
             if (a == NC_NEVER || t - a >= h.kc) continue;
-            const int32_t d = (int32_t)((uint16_t)dly[(size_t)k] & 0x3fffu);
+            const int32_t d = (int32_t)((uint16_t)h.out_delay[(size_t)k] & 0x3fffu);
             const float length_speed = ((float)d * h.dt / 2.0f) * 2.0f;  // length*AP_speed
             const float fire_time = nc::step_ms(a, h.dt);                  // AP_fireTime
             const float start = nc::step_ms(a - d, h.dt);                  // lastSpikeStart
@@ -450,6 +446,8 @@ int nc_get_stats(nc_net* net, nc_stats* out)
     NC_NEED(net);
     if (!out) return fail(NC_ERR_INVALID, "null output");
     unsigned long long s[4];
+    // the dense form counts a step's launches when the next step (or a flush) makes them
+    NC_CALL0(net->eng, flush_plasticity);
     NC_CALL(net->eng, read_stats, 0, s);
     out->fires = (int64_t)s[0];
     out->launched = (int64_t)s[1];

@@ -106,6 +106,7 @@ int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out)
         std::vector<int64_t>().swap(h.in_ptr);
         std::vector<int32_t>().swap(h.ring_off);
         std::vector<int32_t>().swap(h.csc_pre);
+        std::vector<uint16_t>().swap(h.csc_dl);
     }
     *out = b;
     return NC_OK;
@@ -156,6 +157,7 @@ int nc_batch_get_launch(nc_batch* b, nc_launch_config* out)
     out->launch_blocks = b->eng.L.launch_blocks;
     out->launch_block = b->eng.L.launch_block;
     out->graph_steps = b->eng.graph_ticks;
+    out->dense_blocks = b->eng.L.dense_blocks;
     return NC_OK;
 }
 
@@ -165,10 +167,10 @@ int nc_batch_set_launch(nc_batch* b, const nc_launch_config* c)
     // the step kernels are compiled for at most 256 threads per block
     if (!c || c->neuron_block < 32 || c->neuron_block > 256 || c->neuron_block % 32 || c->launch_block < 32 ||
         c->launch_block > 256 || c->launch_block % 32 || c->launch_blocks < 1 || c->launch_blocks > (1 << 20) ||
-        c->graph_steps < 0 || c->graph_steps > 4096)
+        c->graph_steps < 0 || c->graph_steps > 4096 || c->dense_blocks < 0 || c->dense_blocks > (1 << 20))
         return bfail(NC_ERR_INVALID, "bad launch configuration (blocks of 32..256 threads)");
     B_CALL0(b->eng, sync);
-    nc::LaunchShape L{c->neuron_block, c->launch_blocks, c->launch_block};
+    nc::LaunchShape L{c->neuron_block, c->launch_blocks, c->launch_block, c->dense_blocks};
     b->eng.set_launch(L, c->graph_steps);
     return NC_OK;
 }
@@ -180,10 +182,19 @@ int nc_batch_autotune(nc_batch* b, int32_t steps_per_trial, nc_launch_config* be
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->eng.device);
     std::vector<nc_launch_config> cands;
-    for (int nb : {64, 128, 256})
-        for (int lbm : {2, 4, 8})
-            for (int lb : {128, 256})
-                for (int g : {16, 64}) cands.push_back(nc_launch_config{nb, sms * lbm, lb, g});
+    const nc_launch_config cur = {b->eng.L.neuron_block, b->eng.L.launch_blocks, b->eng.L.launch_block,
+                                  b->eng.graph_ticks, b->eng.L.dense_blocks};
+    if (b->eng.dense) {
+        for (int nb : {64, 128, 256})
+            for (int dbm : {0, 2, 4, 8})
+                for (int g : {16, 64})
+                    cands.push_back(nc_launch_config{nb, cur.launch_blocks, cur.launch_block, g, sms * dbm});
+    } else {
+        for (int nb : {64, 128, 256})
+            for (int lbm : {2, 4, 8})
+                for (int lb : {128, 256})
+                    for (int g : {16, 64}) cands.push_back(nc_launch_config{nb, sms * lbm, lb, g, 0});
+    }
     float best_ms = 1e30f;
     nc_launch_config chosen = cands[0];
     for (const auto& c : cands) {
@@ -210,6 +221,7 @@ int nc_batch_get_stats(nc_batch* b, int32_t net, nc_stats* out)
     B_NEED(b);
     if (!out || net < 0 || net >= (int32_t)b->hosts.size()) return bfail(NC_ERR_INVALID, "bad net index");
     unsigned long long s[4];
+    B_CALL0(b->eng, flush_plasticity);  // the dense form's last launches
     B_CALL(b->eng, read_stats, net, s);
     out->fires = (int64_t)s[0];
     out->launched = (int64_t)s[1];

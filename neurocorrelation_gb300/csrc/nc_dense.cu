@@ -1,0 +1,408 @@
+// nc_dense.cu — the dense form of the NeuCor step: a synapse pass and a neuron pass.
+//
+// The event form (nc_kernels.cu) pushes every launched spike from its source into the
+// target's CSC row: scattered term writes and ring atomics per synaptic event.  When a
+// large share of neurons fires every step (the kNN / U[0,1]-weight networks saturate
+// near one fire per refractory period), nearly every in-row is touched every step
+// anyway, and streaming the rows in order is cheaper than scattering into them.
+//
+//   k_dense_synapses (warp per span of 8 x 32 in-synapses, CSC order, coalesced), for
+//   the step prev = t-1 of the span's net:
+//     Synapse::fire of every in-synapse whose source fired at prev (src/NeuCor.cpp:
+//     727-738): dropped while busy, otherwise it captures fl(fl(0.2f*52)*w) and its
+//     arrival step; then the plasticity of prev (src/NeuCor.cpp:740-761): post-spike
+//     branch on the rows of targets that fired at prev, arrival branch on synapses
+//     whose spike arrived at prev.  Launched terms are computed 32 at a time from a
+//     per-warp queue so the two FP64 multiplies run on full warps.  Each chunk's
+//     ballot of "arrived in t-KC .. t-1" is one word of the window bitmap.
+//   k_dense_neurons (lane per neuron): charge_insynapses in ascending source order
+//     from the window bitmap, charge_passive, threshold, AP, background draws (as the
+//     event form's k_neuron_step).
+//
+// Launches of the fires of prev happen at the start of step t instead of the end of
+// step prev; nothing between those points reads what they write (a spike launched at
+// prev arrives at prev+1 at the earliest and joins the fold from prev+2), so the
+// results are the event form's bit for bit.  The launch decision reads the same rule:
+// accepted iff prev - last_arrival >= KC + [target caller id > source caller id], and
+// the captured weight includes the target's post-spike plasticity of prev when the
+// target fired at prev and its caller id is below the source's.  A flush (before
+// read-back) runs the synapse pass early; the step then finds it done (stdp_done) and
+// its window bitmap already written.
+#include "nc_device.cuh"
+#include "nc_engine.cuh"
+
+#include <cuda_runtime.h>
+
+namespace {
+
+using namespace nc_dev;
+
+constexpr int kMaxWarps = 8;  // 256 threads per block at most
+#ifndef NC_DENSE_UNROLL
+#define NC_DENSE_UNROLL 2
+#endif
+constexpr int kUnroll = NC_DENSE_UNROLL;  // chunks whose loads are in flight together
+constexpr int kQueue = 64;                // launched-term queue per warp
+static_assert(NC_SPAN_CHUNKS % kUnroll == 0, "span chunks must be a multiple of the unroll");
+
+struct SynShared {
+    int64_t qs[kMaxWarps][kQueue];  // pool index of the launched synapse
+    float qx[kMaxWarps][kQueue];    // deltaT * AP_depolFac of the launch
+};
+
+__device__ __forceinline__ int warp_sum(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT) for the queued launches [0, count)
+// (src/NeuCor.cpp:695); lane l takes entry l.
+__device__ __forceinline__ void drain_terms(const NcPools& P, const NcNetDesc& D, SynShared& sh, int wib, int lane,
+                                            int count)
+{
+    __syncwarp();
+    if (lane < count) P.term[sh.qs[wib][lane]] = __dmul_rn(__dmul_rn((double)sh.qx[wib][lane], 0.9943), D.e_term);
+    __syncwarp();
+}
+
+// Adds each warp's per-net counters (K of them, into stats[first ..]) to the nets'
+// stats, summed per net over the block first.
+template <int K>
+__device__ void block_counters(const NcPools& P, int* s_net, unsigned long long (*s_acc)[K], int wib, int lane,
+                               int acc_net, const unsigned long long* acc, int first)
+{
+    if (lane == 0) {
+        s_net[wib] = acc_net;
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_acc[wib][k] = acc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int wpb = blockDim.x >> 5;
+        for (int w = 0; w < wpb; ++w) {
+            const int n = s_net[w];
+            if (n < 0) continue;
+            unsigned long long tot[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) tot[k] = s_acc[w][k];
+            for (int v = w + 1; v < wpb; ++v) {
+                if (s_net[v] != n) continue;
+#pragma unroll
+                for (int k = 0; k < K; ++k) tot[k] += s_acc[v][k];
+                s_net[v] = -1;
+            }
+            unsigned long long* st = P.nets[n].stats;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (tot[k]) atomicAdd(st + first + k, tot[k]);
+        }
+    }
+}
+
+template <bool kFlush>
+__global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses(NcPools P)
+{
+    __shared__ SynShared sh;
+    __shared__ int s_net[kMaxWarps];
+    __shared__ unsigned long long s_acc[kMaxWarps][2];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
+
+    int acc_net = -1;
+    unsigned long long acc[2] = {0, 0};  // launched, dropped
+    for (int sp = gw; sp < n_spans; sp += nw) {
+        const NcTile span = P.spans[sp];
+        const NcNetDesc& D = P.nets[span.net];
+        const int32_t t = D.t;
+        const int32_t prev = t - 1;
+        // a flushed step finds its synapse pass done and its window bitmap written; a
+        // net's first step has nothing in flight (the bitmap starts cleared)
+        if (!D.active || prev < 1 || D.stdp_done >= prev) continue;
+        if (!kFlush && t > D.t_end) continue;
+        if (span.net != acc_net) {
+            if (acc_net >= 0 && lane == 0) {
+                unsigned long long* st = P.nets[acc_net].stats;
+                atomicAdd(st + 1, acc[0]);
+                atomicAdd(st + 2, acc[1]);
+            }
+            acc_net = span.net;
+            acc[0] = acc[1] = 0;
+        }
+        const int64_t sb = D.syn_base;
+        const int64_t nsyn = D.n_syn;
+        const int32_t kc = D.kc;
+        const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
+        const int32_t* lfn = P.lf + D.neuron_base;
+        const float* tab_pre = P.tables + D.table_base;
+        const float* tab_post = tab_pre + D.tab_pre_len;
+        int qn = 0, nl = 0, nd = 0;
+        for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
+            int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
+            uint32_t dl[kUnroll], fword[kUnroll], ihw[kUnroll];
+            float wv[kUnroll];
+            bool in[kUnroll];
+            // every load of the pass is issued before the first use
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const int64_t c = span.first + h + u;
+                const int64_t rel = c * 32 + lane;
+                in[u] = rel < nsyn;
+                ihw[u] = 0u;
+                if (in[u]) {
+                    const int64_t s = sb + rel;
+                    pre[u] = __ldg(P.csc_pre + s);
+                    post[u] = __ldg(P.csc_post + s);
+                    dl[u] = __ldg(P.csc_dl + s);
+                    la[u] = P.la_c[s];
+                    wv[u] = P.w[s];
+                    ta[u] = P.t_arr[s];
+                    ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                fword[u] = 0u;
+                lfp[u] = NC_NEVER;
+                if (in[u]) {
+                    fword[u] = fprev[pre[u] >> 5];
+                    lfp[u] = lfn[post[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const int64_t c = span.first + h + u;
+                const int64_t s = sb + c * 32 + lane;
+                int32_t lac = in[u] ? la[u] : NC_NEVER;
+                bool launch = false;
+                float x = 0.0f;
+                if (in[u]) {
+                    const bool tf = lfp[u] == prev;  // target fired at prev
+                    const bool srcf = (fword[u] >> (pre[u] & 31)) & 1u;
+                    const bool arrived = la[u] == prev;
+                    const int32_t after = (int32_t)((dl[u] >> 14) & 1u);
+                    launch = srcf && (la[u] == NC_NEVER || prev - la[u] >= kc + after);
+                    nl += launch;
+                    nd += srcf && !launch;
+                    const bool ih = (ihw[u] >> lane) & 1u;
+                    const float w0 = wv[u];
+                    float w1 = w0;
+                    if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
+                    if (launch) {
+                        // target below the source in caller order and fired at prev: its
+                        // update ran first, post-spike plasticity included
+                        const float cap = (((dl[u] >> 15) & 1u) && tf) ? w1 : w0;
+                        // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                        x = D.dt * (D.c52 * cap);
+                        lac = prev + (int32_t)(dl[u] & 0x3fffu);
+                        P.la_c[s] = lac;
+                    }
+                    float w2 = w1;
+                    if (arrived) {
+                        w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
+                        P.t_arr[s] = prev;
+                    }
+                    if (tf || arrived) P.w[s] = w2;
+                }
+                // arrived t-KC .. t-1: in the fold of step t
+                const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
+                const uint32_t wm = __ballot_sync(kFull, win);
+                if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
+                const uint32_t lm = __ballot_sync(kFull, launch);
+                if (lm) {
+                    if (launch) {
+                        const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                        sh.qs[wib][pos] = s;
+                        sh.qx[wib][pos] = x;
+                    }
+                    qn += __popc(lm);
+                    if (qn >= 32) {
+                        drain_terms(P, D, sh, wib, lane, 32);
+                        if (lane < qn - 32) {
+                            sh.qs[wib][lane] = sh.qs[wib][32 + lane];
+                            sh.qx[wib][lane] = sh.qx[wib][32 + lane];
+                        }
+                        __syncwarp();
+                        qn -= 32;
+                    }
+                }
+            }
+        }
+        if (qn > 0) drain_terms(P, D, sh, wib, lane, qn);
+        acc[0] += (unsigned long long)warp_sum(nl);
+        acc[1] += (unsigned long long)warp_sum(nd);
+    }
+    block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
+}
+
+__global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcPools P)
+{
+    __shared__ int s_net[kMaxWarps];
+    __shared__ unsigned long long s_acc[kMaxWarps][1];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
+
+    int acc_net = -1;
+    unsigned long long acc[1] = {0};  // fires
+    for (int tix = gw; tix < n_tiles; tix += nw) {
+        const NcTile tile = P.tiles[tix];
+        const NcNetDesc& D = P.nets[tile.net];
+        const int32_t t = D.t;
+        if (!(D.active && t <= D.t_end)) continue;
+        if (tile.net != acc_net) {
+            if (acc_net >= 0 && lane == 0) atomicAdd(P.nets[acc_net].stats + 0, acc[0]);
+            acc_net = tile.net;
+            acc[0] = 0;
+        }
+        const int32_t first = tile.first;
+        const int32_t j = first + lane;
+        const bool live = j < D.n;
+        const int32_t pj = D.neuron_base + j;
+        const int64_t word = D.word_base + (first >> 5);
+        const int32_t kc = D.kc;
+        bool fired = false;
+        if (live) {
+            int32_t lf = P.lf[pj];
+            const int64_t s0 = P.in_ptr[D.ptr_base + j];
+            const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
+            float pot = P.pot[pj];
+            const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
+            bool forced = (fw >> lane) & 1u;
+            if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
+            // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
+            // t-1 .. t-KC, ascending source id; the accumulator stays a float value
+            if (s1 > s0) {
+                double pd = (double)pot;
+                const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
+                for (int64_t wa = wa0; wa <= wa1; wa += 2) {
+                    uint32_t x = P.win[wa];
+                    if (wa == wa0) x &= ~0u << (s0 & 31);
+                    if (wa == wa1 && (s1 & 31)) x &= (1u << (s1 & 31)) - 1u;
+                    uint32_t y = 0u;
+                    if (wa + 1 <= wa1) {
+                        y = P.win[wa + 1];
+                        if (wa + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
+                    }
+                    unsigned long long bits = x | ((unsigned long long)y << 32);
+                    const double* tp = P.term + wa * 32;
+                    while (bits) {
+                        int b[8];
+                        pop8_64(&bits, b);
+                        double v[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if (b[k] >= 0) v[k] = tp[b[k]];
+                        pd = fold8(pd, v, b);
+                    }
+                }
+                pot = __double2float_rn(pd);
+            }
+            // charge_passive (src/NeuCor.cpp:677-680)
+            pot = (pot - -70.0f) * D.leak + -70.0f;
+            // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
+            const bool can = (lf == NC_NEVER) || (t - lf >= kc);
+            fired = (-55.0f < pot || forced) && can;
+            if (fired) {
+                lf = t;
+                P.lf[pj] = t;
+                P.firings[pj] += 1u;
+            }
+            // AP (src/NeuCor.cpp:706-714)
+            if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
+            P.pot[pj] = pot;
+        }
+        const uint32_t fmask = __ballot_sync(kFull, fired);
+        if (lane == 0) {
+            P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
+            P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
+            if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
+                D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
+        }
+        acc[0] += (unsigned long long)__popc(fmask);
+        // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
+        if (live && D.bg_period > 0) {
+            uint32_t o[4];
+            philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
+            if (o[0] % (uint32_t)D.bg_period == 0u) {
+                uint32_t tgt = o[1] % (uint32_t)D.n;
+                if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
+                atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
+                         1u << (tgt & 31));
+            }
+        }
+    }
+    block_counters<1>(P, s_net, s_acc, wib, lane, acc_net, acc, 0);
+    // the last block to finish advances the step counters
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(P.done_ctr, 1u) == gridDim.x - 1u);
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int n = threadIdx.x; n < P.n_nets; n += blockDim.x) {
+            NcNetDesc* D = P.nets + n;
+            if (D->active && D->t <= D->t_end) {
+                if (D->stdp_done < D->t - 1) D->stdp_done = D->t - 1;
+                D->stats[3] += 1ull;
+                D->t += 1;
+            }
+        }
+        if (threadIdx.x == 0) *P.done_ctr = 0u;
+    }
+}
+
+// After a flush: the synapse pass of every active net's last step is done.
+__global__ void k_dense_mark_flushed(NcPools P)
+{
+    for (int n = threadIdx.x; n < P.n_nets; n += blockDim.x) {
+        NcNetDesc* D = P.nets + n;
+        if (D->active && D->stdp_done < D->t - 1) D->stdp_done = D->t - 1;
+    }
+}
+
+int syn_blocks(const NcPools& P, const nc::LaunchShape& L)
+{
+    return L.dense_blocks > 0 ? L.dense_blocks : (P.n_spans + kMaxWarps - 1) / kMaxWarps;
+}
+
+}  // namespace
+
+namespace nc {
+
+int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream)
+{
+    const int blocks = syn_blocks(P, L);
+    if (blocks > 0) k_dense_synapses<false><<<blocks, 32 * kMaxWarps, 0, (cudaStream_t)stream>>>(P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
+{
+    const int wpb = L.neuron_block / 32;
+    const int blocks = (P.n_tiles + wpb - 1) / wpb;
+    if (blocks > 0) k_dense_neurons<<<blocks, L.neuron_block, 0, (cudaStream_t)stream>>>(P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream)
+{
+    return launch_dense_synapses(P, L, stream) | launch_dense_neurons(P, L, stream);
+}
+
+int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream)
+{
+    const int blocks = syn_blocks(P, L);
+    if (blocks > 0) k_dense_synapses<true><<<blocks, 32 * kMaxWarps, 0, (cudaStream_t)stream>>>(P);
+    k_dense_mark_flushed<<<1, 256, 0, (cudaStream_t)stream>>>(P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace nc

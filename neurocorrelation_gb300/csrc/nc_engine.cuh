@@ -82,12 +82,15 @@ struct NcNetDesc {
     double e_term;        // 0.9943 is applied separately; this is exp(0.3702*dt) (src/NeuCor.cpp:695)
     uint32_t* raster;     // device raster rows of n_words words
     unsigned long long* stats; // 4 counters: fires, launched, dropped, steps
+    int64_t n_syn;        // synapses (the pool range is padded to a multiple of 32)
 };
 
-struct NcTile {          // 32 consecutive neurons of one net
-    int32_t net;
-    int32_t first;       // local id of the first neuron (multiple of 32)
+struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8 chunks of
+    int32_t net;         // 32 in-synapses
+    int32_t first;       // local id of the first neuron (multiple of 32), or first chunk
 };
+
+constexpr int NC_SPAN_CHUNKS = 8;  // 32-synapse chunks per span of the dense synapse pass
 
 struct NcPools {
     // neurons
@@ -112,6 +115,15 @@ struct NcPools {
     int16_t* out_delay;
     uint32_t* out_ringpos; // (word within slot) << 5 | bit
     int32_t* last_arr;
+    // dense form: in-synapse (CSC) order
+    int32_t* csc_pre;    // source's device slot (local to the net)
+    int32_t* csc_post;   // target's device slot (local to the net)
+    uint16_t* csc_dl;    // delay | target-above-source << 14 | target-below-source << 15
+    int32_t* la_c;       // arrival step of the last accepted launch
+    uint32_t* win;       // bit per synapse: arrived within the fold window of the net's step
+    NcTile* spans;       // work items of the synapse pass
+    int32_t n_spans;
+    int32_t* n_spans_dev; // when set, the span count is read from device memory (served engine)
     // ring and bitsets
     uint32_t* ring;
     uint32_t* fired;     // 2 parities x total_words
@@ -169,14 +181,34 @@ NC_HD inline void nc_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, 
 
 // Kernel launchers (nc_kernels.cu).
 namespace nc {
+// Resident 256-thread blocks per SM the step kernels' register allocation is held to
+// (3 keep every tile of a 100k-neuron net in one wave for the event form's neuron
+// update); the spike-launch grid defaults to NC_LAUNCH_MIN_BLOCKS blocks per SM.
+#ifndef NC_NEURON_MIN_BLOCKS
+#define NC_NEURON_MIN_BLOCKS 3
+#endif
+#ifndef NC_DENSE_MIN_BLOCKS
+#define NC_DENSE_MIN_BLOCKS 4
+#endif
+#ifndef NC_LAUNCH_MIN_BLOCKS
+#define NC_LAUNCH_MIN_BLOCKS 4
+#endif
+
 struct LaunchShape {
     int neuron_block;    // threads per block of the neuron-update kernel (multiple of 32)
     int launch_blocks;   // blocks of the spike-launch kernel
     int launch_block;    // threads per block of the spike-launch kernel
+    int dense_blocks = 0; // blocks of the dense synapse pass (0: one warp per span)
 };
 int launch_neuron_step(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_spike_launch(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_stdp_flush(const NcPools& P, const LaunchShape& L, void* stream);
+// Dense form (nc_dense.cu): the synapse pass and the neuron pass of one step, and the
+// plasticity flush (the synapse pass of the last step's fires) before read-back.
+int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
+int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);
 int launch_raster_to_ids(const uint32_t* in, uint32_t* out, const int32_t* slot_of, int32_t n, int32_t n_words,

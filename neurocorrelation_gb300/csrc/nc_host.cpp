@@ -109,9 +109,12 @@ static void storage_order(NetHost& h, const float* xyz, int32_t order_kind)
 int64_t NetHost::device_bytes() const
 {
     const int64_t per_neuron = 4 + 4 + 4 + 4 + 8 + 8 + 4;             // pot lf firings act_start in_ptr out_ptr ring_off
-    const int64_t per_syn = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 4;            // w t_arr term | out_post out_csc delay ringpos last_arr
+    const bool dense = p.step_mode == NC_STEP_DENSE;
+    // w t_arr term | csc_pre csc_post csc_dl la_c (dense) or out_post out_csc delay ringpos last_arr (event)
+    const int64_t per_syn = 4 + 4 + 8 + (dense ? 4 + 4 + 2 + 4 : 4 + 4 + 2 + 4 + 4);
     const int64_t words = ((int64_t)n + 31) / 32;
-    return per_neuron * (n + 1) + per_syn * s + 4 * (int64_t)ring_slots * ring_words + 4 * 4 * words +
+    const int64_t ring_bytes = dense ? 0 : 4 * (int64_t)ring_slots * ring_words;
+    return per_neuron * (n + 1) + per_syn * s + ring_bytes + 4 * 4 * words +
            8 * 2 * (int64_t)n + 4 * (int64_t)tables.size() + (int64_t)sizeof(NcGroupDev) * (int64_t)groups.size();
 }
 
@@ -187,6 +190,10 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
         err = "unknown storage order";
         return NC_ERR_INVALID;
     }
+    if (p.step_mode != NC_STEP_DENSE && p.step_mode != NC_STEP_EVENT) {
+        err = "unknown step mode";
+        return NC_ERR_INVALID;
+    }
     storage_order(h, xyz, p.storage_order);
 
     // CSC: bucket by target slot in input order, sort each bucket by the caller's source
@@ -250,9 +257,11 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
     h.out_csc.assign((size_t)h.s, 0);
     h.out_delay.assign((size_t)h.s, 0);
     h.out_ringpos.assign((size_t)h.s, 0);
+    h.csc_dl.assign((size_t)h.s, 0);
     {
         std::vector<int64_t> fill(h.out_ptr.begin(), h.out_ptr.end() - 1);
-        std::vector<int32_t> csc_post((size_t)h.s);
+        std::vector<int32_t>& csc_post = h.csc_post;
+        csc_post.assign((size_t)h.s, 0);
         for (int32_t j = 0; j < n; ++j)
             for (int64_t c = h.in_ptr[j]; c < h.in_ptr[j + 1]; ++c) csc_post[(size_t)c] = j;
         for (int64_t k = 0; k < n_syn; ++k) {
@@ -266,6 +275,7 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
             // the same-step order rules compare the caller's ids of target and source
             const uint32_t flags = (to[k] > from[k] ? 1u << kAfterBit : 0u) | (to[k] < from[k] ? 1u << kBeforeBit : 0u);
             h.out_delay[(size_t)q] = (int16_t)(uint16_t)((uint32_t)h.csc_delay[(size_t)c] | flags);
+            h.csc_dl[(size_t)c] = (uint16_t)((uint32_t)h.csc_delay[(size_t)c] | flags);
             h.out_ringpos[(size_t)q] = ((uint32_t)(h.ring_off[j] + (int32_t)(b >> 5)) << 5) | (uint32_t)(b & 31);
         }
     }

@@ -36,6 +36,8 @@ struct NetHost {
     std::vector<float> w;                   // CSC
     std::vector<uint32_t> inh_bits;         // CSC, bit per synapse: Synapse::inhibitory
     std::vector<int32_t> csc_pre, csc_delay;
+    std::vector<uint16_t> csc_dl;           // CSC: delay | flags, as out_delay (dense form)
+    std::vector<int32_t> csc_post;          // CSC: target slot (dense form)
     std::vector<int32_t> out_post, out_csc;
     std::vector<int16_t> out_delay;
     std::vector<uint32_t> out_ringpos;

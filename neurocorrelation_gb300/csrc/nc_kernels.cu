@@ -33,126 +33,41 @@
 // own, as in the reference's x86-64 build.  The reference's transcendentals
 // (powf, exp) are host-built tables indexed by step differences.
 #include "nc_engine.cuh"
+#include "nc_device.cuh"
 
 #include <cuda_runtime.h>
 
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
+using namespace nc_dev;
 
-__device__ __forceinline__ float trace_at(const float* tab, int len, int32_t now, int32_t then)
-{
-    if (then == NC_NEVER) return 0.0f;  // lastSpikeArrival = -inf / lastFire = NaN
-    const int32_t k = now - then;
-    return k < len ? __ldg(tab + k) : 0.0f;
-}
-
-__device__ __forceinline__ bool inh_bit(const NcPools& P, int64_t s)
-{
-    return (__ldg(P.inh + (s >> 5)) >> (s & 31)) & 1u;
-}
-
-// The 32 inhibitory bits of synapses s .. s+31 (s need not be word-aligned; the pool
-// keeps one spare word at its end).
-__device__ __forceinline__ uint32_t inh_bits32(const NcPools& P, int64_t s)
-{
-    const int64_t w0 = s >> 5;
-    return __funnelshift_r(__ldg(P.inh + w0), __ldg(P.inh + w0 + 1), (uint32_t)(s & 31));
-}
-
-// Synapse::synapticPlasticity weight update and clamp (src/NeuCor.cpp:757-761);
-// fmin/fmax keep the C library's generic semantics.
-__device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const NcNetDesc& D)
-{
-    const float weightChange = D.pre_factor * traceS - D.post_factor * traceT;
-    float v = w + weightChange * D.lr;
-    if (!inh) {
-        const float m = (v <= 1.0f) ? v : 1.0f;
-        v = (m >= 0.0f) ? m : 0.0f;
-    } else {
-        const float m = (v <= 0.0f) ? v : 0.0f;
-        v = (m >= -1.0f) ? m : -1.0f;
-    }
-    return v;
-}
-
-// RN32 of a double, returned as the (exactly representable) double: the 52-bit
-// fraction is rounded to 23 bits, half to even, with integer operations.  Values
-// below the float normal range take the hardware conversion.  Together with one
-// double add this is `float += double` (src/NeuCor.cpp:695) with one FP64 operation.
-__device__ __forceinline__ double round_to_float(double d)
-{
-    unsigned long long u = (unsigned long long)__double_as_longlong(d);
-    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
-    if (e < 1023u - 126u) return (double)__double2float_rn(d);
-    u += 0x0FFFFFFFull + ((u >> 29) & 1ull);
-    u &= ~0x1FFFFFFFull;
-    return __longlong_as_double((long long)u);
-}
-
-__device__ __forceinline__ void philox(uint32_t a, uint32_t b, uint32_t stream, uint32_t c, const NcNetDesc& D,
-                                       uint32_t out[4])
-{
-    nc_philox(a, b, stream, c, D.key0, D.key1, out);
-}
-
-// Whether input neuron j requests a fire at step t (Poisson groups).
-__device__ bool input_request(const NcPools& P, const NcNetDesc& D, int32_t j, int32_t t)
-{
-    uint32_t o[4];
-    for (int g = 0; g < D.n_groups; ++g) {
-        const NcGroupDev G = P.groups[D.group_base + g];
-        if (j < G.first || j >= G.first + G.count) continue;
-        const uint32_t m = (uint32_t)(j - G.first);
-        if (!G.correlated) {
-            philox((uint32_t)G.index, (uint32_t)t, NC_STREAM_INDEPENDENT, m, D, o);
-            if (o[0] < G.thresh) return true;
-            continue;
-        }
-        for (int32_t src = t - G.jitter; src <= t + G.jitter; ++src) {
-            if (src < 0) continue;
-            philox((uint32_t)G.index, (uint32_t)src, NC_STREAM_SOURCE, 0u, D, o);
-            if (!(o[0] < G.thresh)) continue;
-            philox((uint32_t)G.index, (uint32_t)src, NC_STREAM_JITTER, m, D, o);
-            const int32_t off = (int32_t)(o[0] % (uint32_t)(2 * G.jitter + 1)) - G.jitter;
-            if (src + off == t) return true;
-        }
-    }
-    return false;
-}
-
-// Pops up to 8 set bits of *m in ascending order into b[] (-1 when exhausted).
-__device__ __forceinline__ void pop8(uint32_t* m, int b[8])
-{
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        b[k] = *m ? __ffs(*m) - 1 : -1;
-        *m &= *m - 1u;
-    }
-}
-
-// Deferred plasticity of step `prev` for the 32 neurons of a tile (all lanes call).
-__device__ void tile_plasticity(const NcPools& P, const NcNetDesc& D, int64_t word, int lane, bool live,
-                                int64_t s0, int64_t s1, int32_t r0, int32_t r1, int32_t lf, int32_t prev)
+// Post-spike branch of the plasticity of step `prev` (src/NeuCor.cpp:650-655, 740-761):
+// the whole in-row of every neuron of the tile that fired at prev.  The warp takes the
+// rows two at a time, each lane four synapses of each, so eight loads per lane are in
+// flight per pass (all lanes call).
+__device__ void postfire_rows(const NcPools& P, const NcNetDesc& D, int64_t word, int lane, int64_t s0, int64_t s1,
+                              int32_t prev)
 {
     const float* tab_pre = P.tables + D.table_base;
-    const float* tab_post = tab_pre + D.tab_pre_len;
-    // post-spike branch: the whole in-row of each neuron that fired at prev, the warp
-    // striding it four chunks at a time so the loads of a chunk group overlap
     uint32_t m = P.fired[(int64_t)(prev & 1) * P.total_words + word];
     while (m) {
-        const int b = __ffs(m) - 1;
+        const int ba = __ffs(m) - 1;
         m &= m - 1;
-        const int64_t a0 = __shfl_sync(kFull, s0, b);
-        const int64_t a1 = __shfl_sync(kFull, s1, b);
-        for (int64_t base = a0; base < a1; base += 128) {
-            float wv[4];
-            int32_t ta[4];
-            bool ok[4], ih[4];
+        const bool pair = m != 0;
+        const int bb = pair ? __ffs(m) - 1 : ba;
+        if (pair) m &= m - 1;
+        const int64_t a0 = __shfl_sync(kFull, s0, ba), a1 = __shfl_sync(kFull, s1, ba);
+        const int64_t c0 = __shfl_sync(kFull, s0, bb);
+        const int64_t c1 = pair ? __shfl_sync(kFull, s1, bb) : c0;
+        const int64_t len = (a1 - a0) > (c1 - c0) ? (a1 - a0) : (c1 - c0);
+        for (int64_t off = 0; off < len; off += 128) {
+            float wv[8];
+            int32_t ta[8];
+            bool ok[8], ih[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t s = base + lane + 32 * u;
-                ok[u] = s < a1;
+            for (int u = 0; u < 8; ++u) {
+                const int64_t s = (u < 4 ? a0 : c0) + off + lane + 32 * (u & 3);
+                ok[u] = s < (u < 4 ? a1 : c1);
                 if (ok[u]) {
                     wv[u] = P.w[s];
                     ta[u] = P.t_arr[s];
@@ -160,42 +75,48 @@ __device__ void tile_plasticity(const NcPools& P, const NcNetDesc& D, int64_t wo
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 if (!ok[u]) continue;
-                const int64_t s = base + lane + 32 * u;
+                const int64_t s = (u < 4 ? a0 : c0) + off + lane + 32 * (u & 3);
                 P.w[s] = plasticity(wv[u], ih[u], trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
             }
         }
     }
     __syncwarp();
-    // arrival branch: spikes that arrived at prev (lastSpikeArrival = now; traceS = 0)
-    if (live && r1 > r0) {
-        const uint32_t* slot = P.ring + D.ring_base + (int64_t)(prev & D.ring_mask) * D.ring_words;
-        const float trT = trace_at(tab_post, D.tab_post_len, prev, lf);
-        for (int32_t wi = r0; wi < r1; ++wi) {
-            uint32_t bits = slot[wi];
-            if (!bits) continue;
-            const int64_t cs = s0 + (int64_t)(wi - r0) * 32;
-            const uint32_t ih = inh_bits32(P, cs);
-            while (bits) {
-                int b[8];
-                pop8(&bits, b);
-                float wv[8];
+}
+
+// Arrival branch of the plasticity of step `prev` (Synapse::run, src/NeuCor.cpp:718-726:
+// lastSpikeArrival = now, so traceS = 0) for one lane's in-row; used when the
+// plasticity is flushed outside the step.
+__device__ void arrival_row(const NcPools& P, const NcNetDesc& D, int64_t s0, int32_t r0, int32_t r1, int32_t lf,
+                            int32_t prev)
+{
+    const float* tab_post = P.tables + D.table_base + D.tab_pre_len;
+    const uint32_t* slot = P.ring + D.ring_base + (int64_t)(prev & D.ring_mask) * D.ring_words;
+    const float trT = trace_at(tab_post, D.tab_post_len, prev, lf);
+    for (int32_t wi = r0; wi < r1; ++wi) {
+        uint32_t bits = slot[wi];
+        if (!bits) continue;
+        const int64_t cs = s0 + (int64_t)(wi - r0) * 32;
+        const uint32_t ih = inh_bits32(P, cs);
+        while (bits) {
+            int b[8];
+            pop8(&bits, b);
+            float wv[8];
 #pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    if (b[k] >= 0) wv[k] = P.w[cs + b[k]];
+            for (int k = 0; k < 8; ++k)
+                if (b[k] >= 0) wv[k] = P.w[cs + b[k]];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    if (b[k] < 0) continue;
-                    P.t_arr[cs + b[k]] = prev;
-                    P.w[cs + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1u, 0.0f, trT, D);
-                }
+            for (int k = 0; k < 8; ++k) {
+                if (b[k] < 0) continue;
+                P.t_arr[cs + b[k]] = prev;
+                P.w[cs + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1u, 0.0f, trT, D);
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
+__global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPools P)
 {
     __shared__ int s_cnt[32];
     __shared__ int s_base;
@@ -226,49 +147,88 @@ __global__ void __launch_bounds__(256) k_neuron_step(NcPools P)
             int32_t lf = NC_NEVER;
             int64_t s0 = 0, s1 = 0;
             int32_t r0 = 0, r1 = 0;
+            float pot = 0.0f;
+            uint32_t fw = 0;
             if (live) {
                 lf = P.lf[pj];
                 s0 = P.in_ptr[pb];
                 s1 = P.in_ptr[pb + 1];
                 r0 = P.ring_off[pb];
                 r1 = P.ring_off[pb + 1];
+                pot = P.pot[pj];
+                fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
             }
             const int32_t prev = t - 1;
-            if (prev >= 1 && D.stdp_done < prev) tile_plasticity(P, D, word, lane, live, s0, s1, r0, r1, lf, prev);
+            const bool stdp = prev >= 1 && D.stdp_done < prev;
+            if (stdp) postfire_rows(P, D, word, lane, s0, s1, prev);
 
             bool fired = false;
             if (live) {
-                const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
                 bool forced = (fw >> lane) & 1u;
                 if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
                 // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
-                // t-1 .. t-KC, ascending source id; the accumulator stays a float value
-                float pot = P.pot[pj];
+                // t-1 .. t-KC, ascending source id; the accumulator stays a float value.
+                // The arrival branch of the deferred plasticity rides along: the spikes
+                // that arrived at prev are the ring bits of slot prev.
                 if (r1 > r0) {
                     uint32_t* ring = P.ring + D.ring_base;
-                    const int32_t oldest = t - D.kc;
+                    const int64_t rw = D.ring_words;
+                    const int32_t kc = D.kc;
+                    const int32_t oldest = t - kc;
+                    const float trT = trace_at(P.tables + D.table_base + D.tab_pre_len, D.tab_post_len, prev, lf);
                     double pd = (double)pot;
-                    for (int32_t wi = r0; wi < r1; ++wi) {
-                        uint32_t bits = 0, last = 0;
-                        for (int32_t k = 1; k <= D.kc; ++k) {
-                            if (t - k < 1) break;
-                            last = ring[(int64_t)((t - k) & D.ring_mask) * D.ring_words + wi];
-                            bits |= last;
+                    for (int32_t wi = r0; wi < r1; wi += 2) {
+                        const bool two = wi + 1 < r1;
+                        uint32_t lo = 0, hi = 0, alo = 0, ahi = 0, olo = 0, ohi = 0;
+                        for (int32_t k = 1; k <= kc && t - k >= 1; ++k) {
+                            const uint32_t* row = ring + (int64_t)((t - k) & D.ring_mask) * rw + wi;
+                            const uint32_t x = row[0];
+                            const uint32_t y = two ? row[1] : 0u;
+                            lo |= x;
+                            hi |= y;
+                            if (k == 1) {
+                                alo = x;
+                                ahi = y;
+                            }
+                            olo = x;  // ends as the word of slot t-KC when t-KC >= 1
+                            ohi = y;
                         }
-                        const double* tp = P.term + s0 + (int64_t)(wi - r0) * 32;
+                        unsigned long long bits = lo | ((unsigned long long)hi << 32);
+                        const unsigned long long arr = stdp ? (alo | ((unsigned long long)ahi << 32)) : 0ull;
+                        const int64_t sb = s0 + (int64_t)(wi - r0) * 32;
+                        unsigned long long ih = 0ull;
+                        if (arr) ih = inh_bits32(P, sb) | ((unsigned long long)(two ? inh_bits32(P, sb + 32) : 0u) << 32);
+                        // arrival branch first (it touches w and t_arr only, the fold reads term)
+                        unsigned long long am = arr;
+                        while (am) {
+                            int b[8];
+                            pop8_64(&am, b);
+                            float wv[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (b[k] >= 0) wv[k] = P.w[sb + b[k]];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                if (b[k] < 0) continue;
+                                P.t_arr[sb + b[k]] = prev;
+                                P.w[sb + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1ull, 0.0f, trT, D);
+                            }
+                        }
                         while (bits) {
                             int b[8];
-                            pop8(&bits, b);
+                            pop8_64(&bits, b);
                             double v[8];
 #pragma unroll
                             for (int k = 0; k < 8; ++k)
-                                if (b[k] >= 0) v[k] = tp[b[k]];
-#pragma unroll
-                            for (int k = 0; k < 8; ++k)
-                                if (b[k] >= 0) pd = round_to_float(__dadd_rn(pd, v[k]));
+                                if (b[k] >= 0) v[k] = P.term[sb + b[k]];
+                            pd = fold8(pd, v, b);
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
-                        if (oldest >= 1 && last) ring[(int64_t)(oldest & D.ring_mask) * D.ring_words + wi] = 0u;
+                        if (oldest >= 1) {
+                            uint32_t* orow = ring + (int64_t)(oldest & D.ring_mask) * rw + wi;
+                            if (olo) orow[0] = 0u;
+                            if (two && ohi) orow[1] = 0u;
+                        }
                     }
                     pot = __double2float_rn(pd);
                 }
@@ -335,7 +295,7 @@ __device__ __forceinline__ int warp_sum(int v)
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_spike_launch(NcPools P)
+__global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPools P)
 {
     __shared__ int s_last;
     __shared__ int s_net[32];
@@ -499,7 +459,8 @@ __global__ void __launch_bounds__(256) k_stdp_flush(NcPools P)
         r0 = P.ring_off[pb];
         r1 = P.ring_off[pb + 1];
     }
-    tile_plasticity(P, D, D.word_base + (tile.first >> 5), lane, live, s0, s1, r0, r1, lf, prev);
+    postfire_rows(P, D, D.word_base + (tile.first >> 5), lane, s0, s1, prev);
+    if (live && r1 > r0) arrival_row(P, D, s0, r0, r1, lf, prev);
 }
 
 __global__ void k_mark_flushed(NcPools P)

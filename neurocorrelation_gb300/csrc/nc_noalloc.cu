@@ -6,9 +6,9 @@
 // allocated, and replays CUDA graphs it instantiates on first use.  Code that records
 // the step into its own CUDA graph, or runs under a fixed device-memory budget, cannot
 // let the library allocate or instantiate anything per call.  nc_run_noalloc launches
-// the same two kernels directly and gives them a scratch area that lives in this file's
-// static device array instead: nothing is allocated, the network's own arrays are the
-// inputs and outputs.
+// the same kernels directly.  The event form gets a scratch area that lives in this
+// file's static device array instead; the dense form needs none.  Nothing is
+// allocated, the network's own arrays are the inputs and outputs.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -61,31 +61,39 @@ extern "C" int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream)
     if (!net) return nc::set_last_error(NC_ERR_INVALID, "null handle");
     if (n_steps < 0) return nc::set_last_error(NC_ERR_INVALID, "negative step count");
     if (net->step + n_steps >= (1ll << 30)) return nc::set_last_error(NC_ERR_INVALID, "step counter limit reached");
-    const int64_t neurons = net->eng.P.fired_cap;
-    if (neurons > kMaxNeurons)
-        return nc::set_last_error(NC_ERR_INVALID, "nc_run_noalloc serves networks of at most " +
-                                                      std::to_string(kMaxNeurons) + " neurons; this one has " +
-                                                      std::to_string(neurons) + " (use nc_run)");
     cudaError_t e = cudaSetDevice(net->eng.device);
     if (e != cudaSuccess) return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("cudaSetDevice", e));
-    NoallocScratch* scratch = nullptr;
-    const int rc = scratch_for(net->eng.device, &scratch);
-    if (rc != NC_OK) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : net->eng.stream;
-
-    // the same kernels and network arrays as nc_run; only the scratch moves
-    NcPools P = net->eng.P;
-    P.fired_list = scratch->fired_list;
-    P.fired_count = scratch->fired_count;
-    P.tick = &scratch->tick;
-    P.done_ctr = &scratch->done_ctr;
-    P.fired_cap = kMaxNeurons;
-    // the array keeps the previous call's contents: the counters must start at zero
-    e = cudaMemsetAsync(scratch->fired_count, 0, sizeof(int32_t) * 2 + sizeof(int32_t) + sizeof(uint32_t), s);
-    if (e != cudaSuccess) return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("cudaMemsetAsync(noalloc counters)", e));
-    for (int32_t k = 0; k < n_steps; ++k) {
-        if (nc::launch_neuron_step(P, net->eng.L, s) || nc::launch_spike_launch(P, net->eng.L, s))
-            return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("nc_run_noalloc launch", cudaGetLastError()));
+    if (net->eng.dense) {
+        // the dense form keeps no scratch between its launches: the network's own arrays
+        // are all it reads and writes
+        for (int32_t k = 0; k < n_steps; ++k)
+            if (nc::launch_step_dense(net->eng.P, net->eng.L, s))
+                return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("nc_run_noalloc launch", cudaGetLastError()));
+    } else {
+        const int64_t neurons = net->eng.P.fired_cap;
+        if (neurons > kMaxNeurons)
+            return nc::set_last_error(NC_ERR_INVALID, "nc_run_noalloc serves event-form networks of at most " +
+                                                          std::to_string(kMaxNeurons) + " neurons; this one has " +
+                                                          std::to_string(neurons) + " (use nc_run)");
+        NoallocScratch* scratch = nullptr;
+        const int rc = scratch_for(net->eng.device, &scratch);
+        if (rc != NC_OK) return rc;
+        // the same kernels and network arrays as nc_run; only the scratch moves
+        NcPools P = net->eng.P;
+        P.fired_list = scratch->fired_list;
+        P.fired_count = scratch->fired_count;
+        P.tick = &scratch->tick;
+        P.done_ctr = &scratch->done_ctr;
+        P.fired_cap = kMaxNeurons;
+        // the array keeps the previous call's contents: the counters must start at zero
+        e = cudaMemsetAsync(scratch->fired_count, 0, sizeof(int32_t) * 2 + sizeof(int32_t) + sizeof(uint32_t), s);
+        if (e != cudaSuccess)
+            return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("cudaMemsetAsync(noalloc counters)", e));
+        for (int32_t k = 0; k < n_steps; ++k) {
+            if (nc::launch_neuron_step(P, net->eng.L, s) || nc::launch_spike_launch(P, net->eng.L, s))
+                return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("nc_run_noalloc launch", cudaGetLastError()));
+        }
     }
     net->step += n_steps;
     for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;

@@ -93,10 +93,11 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     L.neuron_block = 256;
     L.launch_block = 256;
-    L.launch_blocks = std::max(1, sms * 4);
+    L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
+    dense = nets.empty() || nets[0]->p.step_mode == NC_STEP_DENSE;
 
     // pool sizes
-    int64_t neurons = 0, ptrs = 0, words = 0, syn = 0, ring = 0, tables = 0, tiles = 0;
+    int64_t neurons = 0, ptrs = 0, words = 0, syn = 0, ring = 0, tables = 0, tiles = 0, spans = 0;
     const int ngroups_each = std::max(group_capacity, 1);
     slots.clear();
     std::vector<NcNetDesc> desc;
@@ -147,15 +148,17 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         d.pre_factor = h.p.presynaptic_factor;
         d.post_factor = h.p.postsynaptic_factor;
         d.e_term = h.e_term;
+        d.n_syn = h.s;
         desc.push_back(d);
         slots.push_back(sl);
         neurons += h.n;
         ptrs += h.n + 1;
         words += sl.n_words;
         syn += (h.s + 31) / 32 * 32;  // keeps every net's inhibitory bits word-aligned
-        ring += (int64_t)h.ring_slots * h.ring_words;
+        if (!dense) ring += (int64_t)h.ring_slots * h.ring_words;
         tables += (int64_t)h.tables.size();
         tiles += sl.n_words;
+        spans += ((h.s + 31) / 32 + NC_SPAN_CHUNKS - 1) / NC_SPAN_CHUNKS;
         if (h.groups.size() > (size_t)ngroups_each) {
             err = "more input groups than reserved";
             return NC_ERR_INVALID;
@@ -173,23 +176,32 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(P.orig_id, int32_t, neurons);
     NC_ALLOC(P.slot_of, int32_t, neurons);
     NC_ALLOC(P.in_ptr, int64_t, ptrs);
-    NC_ALLOC(P.out_ptr, int64_t, ptrs);
-    NC_ALLOC(P.ring_off, int32_t, ptrs);
     NC_ALLOC(P.w, float, syn);
     NC_ALLOC(P.inh, uint32_t, (syn + 31) / 32 + 1);  // one spare word for 32-bit windows
     NC_ALLOC(P.t_arr, int32_t, syn);
     NC_ALLOC(P.term, double, syn);
-    NC_ALLOC(P.out_post, int32_t, syn);
-    NC_ALLOC(P.out_csc, int32_t, syn);
-    NC_ALLOC(P.out_delay, int16_t, syn);
-    NC_ALLOC(P.out_ringpos, uint32_t, syn);
-    NC_ALLOC(P.last_arr, int32_t, syn);
-    NC_ALLOC(P.ring, uint32_t, ring);
+    if (dense) {
+        NC_ALLOC(P.csc_pre, int32_t, syn);
+        NC_ALLOC(P.csc_post, int32_t, syn);
+        NC_ALLOC(P.csc_dl, uint16_t, syn);
+        NC_ALLOC(P.la_c, int32_t, syn);
+        NC_ALLOC(P.win, uint32_t, syn / 32 + 1);
+        NC_ALLOC(P.spans, NcTile, spans);
+    } else {
+        NC_ALLOC(P.out_ptr, int64_t, ptrs);
+        NC_ALLOC(P.ring_off, int32_t, ptrs);
+        NC_ALLOC(P.out_post, int32_t, syn);
+        NC_ALLOC(P.out_csc, int32_t, syn);
+        NC_ALLOC(P.out_delay, int16_t, syn);
+        NC_ALLOC(P.out_ringpos, uint32_t, syn);
+        NC_ALLOC(P.last_arr, int32_t, syn);
+        NC_ALLOC(P.ring, uint32_t, ring);
+    }
     P.total_words = std::max<int64_t>(words, 1);
     NC_ALLOC(P.fired, uint32_t, 2 * P.total_words);
     NC_ALLOC(P.forced, uint32_t, 2 * P.total_words);
-    P.fired_cap = std::max<int64_t>(neurons, 1);
-    NC_ALLOC(P.fired_list, int2, 2 * P.fired_cap);
+    P.fired_cap = dense ? 0 : std::max<int64_t>(neurons, 1);
+    if (!dense) NC_ALLOC(P.fired_list, int2, 2 * P.fired_cap);
     NC_ALLOC(P.fired_count, int32_t, 2);
     NC_ALLOC(P.tables, float, tables);
     NC_ALLOC(P.groups, NcGroupDev, nets.size() * ngroups_each);
@@ -200,9 +212,10 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(d_stats_, unsigned long long, 4 * nets.size());
     P.n_nets = (int32_t)nets.size();
     P.n_tiles = (int32_t)tiles;
+    P.n_spans = dense ? (int32_t)spans : 0;
 
     // contents
-    std::vector<NcTile> tile_host;
+    std::vector<NcTile> tile_host, span_host;
     tile_host.reserve((size_t)tiles);
     for (size_t q = 0; q < nets.size(); ++q) {
         const NetHost& h = *nets[q];
@@ -219,17 +232,26 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         for (auto& v : inp) v += sl.syn_base;
         for (auto& v : outp) v += sl.syn_base;
         NC_CK(upload(P.in_ptr, inp, sl.ptr_base, stream));
-        NC_CK(upload(P.out_ptr, outp, sl.ptr_base, stream));
-        NC_CK(upload(P.ring_off, h.ring_off, sl.ptr_base, stream));
         NC_CK(upload(P.w, h.w, sl.syn_base, stream));
         NC_CK(upload(P.inh, h.inh_bits, sl.syn_base / 32, stream));
         std::vector<int32_t> never((size_t)h.s, NC_NEVER);
         NC_CK(upload(P.t_arr, never, sl.syn_base, stream));
-        NC_CK(upload(P.last_arr, never, sl.syn_base, stream));
-        NC_CK(upload(P.out_post, h.out_post, sl.syn_base, stream));
-        NC_CK(upload(P.out_csc, h.out_csc, sl.syn_base, stream));
-        NC_CK(upload(P.out_delay, h.out_delay, sl.syn_base, stream));
-        NC_CK(upload(P.out_ringpos, h.out_ringpos, sl.syn_base, stream));
+        if (dense) {
+            NC_CK(upload(P.csc_pre, h.csc_pre, sl.syn_base, stream));
+            NC_CK(upload(P.csc_post, h.csc_post, sl.syn_base, stream));
+            NC_CK(upload(P.csc_dl, h.csc_dl, sl.syn_base, stream));
+            NC_CK(upload(P.la_c, never, sl.syn_base, stream));
+            const int32_t chunks = (int32_t)((h.s + 31) / 32);
+            for (int32_t c = 0; c < chunks; c += NC_SPAN_CHUNKS) span_host.push_back(NcTile{(int32_t)q, c});
+        } else {
+            NC_CK(upload(P.out_ptr, outp, sl.ptr_base, stream));
+            NC_CK(upload(P.ring_off, h.ring_off, sl.ptr_base, stream));
+            NC_CK(upload(P.last_arr, never, sl.syn_base, stream));
+            NC_CK(upload(P.out_post, h.out_post, sl.syn_base, stream));
+            NC_CK(upload(P.out_csc, h.out_csc, sl.syn_base, stream));
+            NC_CK(upload(P.out_delay, h.out_delay, sl.syn_base, stream));
+            NC_CK(upload(P.out_ringpos, h.out_ringpos, sl.syn_base, stream));
+        }
         NC_CK(upload(P.tables, h.tables, d.table_base, stream));
         if (!h.groups.empty()) NC_CK(upload(P.groups, h.groups, sl.group_base, stream));
         for (int32_t f = 0; f < h.n; f += 32) tile_host.push_back(NcTile{(int32_t)q, f});
@@ -238,6 +260,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     }
     NC_CK(upload(P.nets, desc, 0, stream));
     NC_CK(upload(P.tiles, tile_host, 0, stream));
+    if (dense) NC_CK(upload(P.spans, span_host, 0, stream));
     NC_CK(cudaStreamSynchronize(stream));
     for (size_t q = 0; q < nets.size(); ++q) {
         if (launch_background_prologue(P, (int)q, nets[q]->n, stream) != 0) {
@@ -261,10 +284,7 @@ int Engine::capture_graph(std::string& err)
     cudaGraph_t g = nullptr;
     NC_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
-    for (int k = 0; k < graph_ticks && rc == 0; ++k) {
-        rc |= launch_neuron_step(P, L, stream);
-        rc |= launch_spike_launch(P, L, stream);
-    }
+    for (int k = 0; k < graph_ticks && rc == 0; ++k) rc |= launch_tick(stream);
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (rc != 0 || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -295,12 +315,18 @@ int Engine::step(int64_t ticks, std::string& err)
         }
     }
     for (int64_t k = 0; k < ticks; ++k) {
-        if (launch_neuron_step(P, L, stream) || launch_spike_launch(P, L, stream)) {
+        if (launch_tick(stream)) {
             err = cuda_msg("step launch", cudaGetLastError());
             return NC_ERR_CUDA;
         }
     }
     return NC_OK;
+}
+
+int Engine::launch_tick(cudaStream_t s)
+{
+    if (dense) return launch_step_dense(P, L, s);
+    return launch_neuron_step(P, L, s) | launch_spike_launch(P, L, s);
 }
 
 int Engine::step_timed(int64_t ticks, float* ms, std::string& err)
@@ -326,9 +352,15 @@ int Engine::time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::str
     for (auto& e : ev) NC_CK(cudaEventCreate(&e));
     for (int k = 0; k < ticks; ++k) {
         NC_CK(cudaEventRecord(ev[3 * k], stream));
-        if (launch_neuron_step(P, L, stream)) { err = "launch"; return NC_ERR_CUDA; }
+        if (dense ? launch_dense_synapses(P, L, stream) : launch_neuron_step(P, L, stream)) {
+            err = "launch";
+            return NC_ERR_CUDA;
+        }
         NC_CK(cudaEventRecord(ev[3 * k + 1], stream));
-        if (launch_spike_launch(P, L, stream)) { err = "launch"; return NC_ERR_CUDA; }
+        if (dense ? launch_dense_neurons(P, L, stream) : launch_spike_launch(P, L, stream)) {
+            err = "launch";
+            return NC_ERR_CUDA;
+        }
         NC_CK(cudaEventRecord(ev[3 * k + 2], stream));
     }
     NC_CK(cudaStreamSynchronize(stream));
@@ -348,7 +380,7 @@ int Engine::time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::str
 
 int Engine::flush_plasticity(std::string& err)
 {
-    if (launch_stdp_flush(P, L, stream)) {
+    if (dense ? launch_flush_dense(P, L, stream) : launch_stdp_flush(P, L, stream)) {
         err = cuda_msg("plasticity flush", cudaGetLastError());
         return NC_ERR_CUDA;
     }

@@ -38,6 +38,7 @@ public:
     int step_timed(int64_t ticks, float* ms, std::string& err);
     // Mean device time of one neuron-update and one spike-launch launch over `ticks`
     // individually timed ticks (these ticks also advance the nets).
+    // (dense form: the synapse pass and the neuron pass)
     int time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::string& err);
     int flush_plasticity(std::string& err);
     int sync(std::string& err);
@@ -58,6 +59,9 @@ public:
     cudaStream_t stream = nullptr;
     int device = 0;
     int graph_ticks = 32;
+    bool dense = true;  // NC_STEP_DENSE: one launch per step (nc_dense.cu)
+    // Launches one tick of the engine's form on `s` (no graph).
+    int launch_tick(cudaStream_t s);
 
 private:
     int capture_graph(std::string& err);

@@ -111,7 +111,9 @@ struct Kept {
 };
 
 constexpr int kGroupsPerNet = 16;
-constexpr double kSynBytes = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 4 + 0.125;  // w t_arr term | out_* last_arr | inh
+// per synapse: w t_arr term inh | out_* last_arr (event form) or csc_pre csc_dl la_c (dense)
+constexpr double kSynBytesEvent = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 4 + 0.125;
+constexpr double kSynBytesDense = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 0.125 + 0.125;  // + csc_post, window bit
 constexpr double kNeuronBytes = 4 * 6 + 16 + 20 + 0.5 + 0.25;         // state, fired list, pointers, bitsets, tiles
 
 }  // namespace
@@ -124,10 +126,14 @@ struct nc_server {
     nc::LaunchShape L{};
     std::vector<void*> allocs;
     int64_t syn_cap = 0, neuron_cap = 0, ptr_cap = 0, word_cap = 0, ring_cap = 0, table_cap = 0, tile_cap = 0;
+    bool dense = true;
+    double syn_bytes = kSynBytesDense;
     RangeAlloc a_neuron, a_ptr, a_word, a_syn, a_ring, a_table;
     std::vector<int32_t> free_slots;
     unsigned long long* d_stats = nullptr;
     int32_t* d_ntiles = nullptr;
+    int32_t* d_nspans = nullptr;
+    int64_t span_cap = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -190,18 +196,23 @@ int nc_server::init(std::string& err)
     S_CK(cudaEventCreate(&ev1));
     int sms = 0;
     S_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    // pool capacities carved from the budget: ~80% synapse arrays, the rest neurons,
-    // ring buffers and tables (fan-out of at least 16 assumed for the neuron share)
+    // pool capacities carved from the budget: the trace/AP tables first (~600 floats per
+    // network at dt = 1 ms), then ~80% (event form) or ~87% (dense form, which keeps no
+    // ring buffers) of the rest for synapse arrays, then neurons (fan-out of at least 16
+    // assumed) and the event form's ring buffers
     const double budget = (double)cfg.memory_budget_bytes;
-    syn_cap = (int64_t)(0.80 * budget / kSynBytes) / 32 * 32;
-    neuron_cap = std::max<int64_t>(1024, syn_cap / 16);
+    dense = cfg.step_mode == NC_STEP_DENSE;
+    syn_bytes = dense ? kSynBytesDense : kSynBytesEvent;
     const int32_t nets = cfg.max_networks;
+    table_cap = (int64_t)nets * 8192 + 65536;
+    const double avail = budget - 4.0 * (double)table_cap;
+    syn_cap = avail > 0 ? (int64_t)((dense ? 0.87 : 0.80) * avail / syn_bytes) / 32 * 32 : 0;
+    neuron_cap = std::max<int64_t>(1024, syn_cap / 16);
     ptr_cap = neuron_cap + nets;
     word_cap = neuron_cap / 32 + nets;
     tile_cap = word_cap;
-    ring_cap = (int64_t)(0.07 * budget / 4.0);
-    table_cap = (int64_t)nets * 8192 + 65536;  // trace and AP tables: ~600 floats per network at dt = 1 ms
-    const double used = syn_cap * kSynBytes + neuron_cap * kNeuronBytes + ring_cap * 4.0 + table_cap * 4.0;
+    ring_cap = dense ? 0 : (int64_t)(0.07 * budget / 4.0);
+    const double used = syn_cap * syn_bytes + neuron_cap * kNeuronBytes + ring_cap * 4.0 + table_cap * 4.0;
     if (syn_cap < 32 || used > 1.05 * budget) {
         err = "memory budget too small";
         return NC_ERR_BUDGET;
@@ -216,23 +227,34 @@ int nc_server::init(std::string& err)
     S_AL(P.orig_id, int32_t, neuron_cap);
     S_AL(P.slot_of, int32_t, neuron_cap);
     S_AL(P.in_ptr, int64_t, ptr_cap);
-    S_AL(P.out_ptr, int64_t, ptr_cap);
-    S_AL(P.ring_off, int32_t, ptr_cap);
     S_AL(P.w, float, syn_cap);
     S_AL(P.inh, uint32_t, syn_cap / 32 + 1);
     S_AL(P.t_arr, int32_t, syn_cap);
     S_AL(P.term, double, syn_cap);
-    S_AL(P.out_post, int32_t, syn_cap);
-    S_AL(P.out_csc, int32_t, syn_cap);
-    S_AL(P.out_delay, int16_t, syn_cap);
-    S_AL(P.out_ringpos, uint32_t, syn_cap);
-    S_AL(P.last_arr, int32_t, syn_cap);
-    S_AL(P.ring, uint32_t, ring_cap);
+    if (dense) {
+        span_cap = syn_cap / (32 * NC_SPAN_CHUNKS) + nets;
+        S_AL(P.csc_pre, int32_t, syn_cap);
+        S_AL(P.csc_post, int32_t, syn_cap);
+        S_AL(P.csc_dl, uint16_t, syn_cap);
+        S_AL(P.la_c, int32_t, syn_cap);
+        S_AL(P.win, uint32_t, syn_cap / 32 + 1);
+        S_AL(P.spans, NcTile, span_cap);
+        S_AL(d_nspans, int32_t, 1);
+    } else {
+        S_AL(P.out_ptr, int64_t, ptr_cap);
+        S_AL(P.ring_off, int32_t, ptr_cap);
+        S_AL(P.out_post, int32_t, syn_cap);
+        S_AL(P.out_csc, int32_t, syn_cap);
+        S_AL(P.out_delay, int16_t, syn_cap);
+        S_AL(P.out_ringpos, uint32_t, syn_cap);
+        S_AL(P.last_arr, int32_t, syn_cap);
+        S_AL(P.ring, uint32_t, ring_cap);
+    }
     P.total_words = word_cap;
     S_AL(P.fired, uint32_t, 2 * word_cap);
     S_AL(P.forced, uint32_t, 2 * word_cap);
-    P.fired_cap = neuron_cap;
-    S_AL(P.fired_list, int2, 2 * neuron_cap);
+    P.fired_cap = dense ? 0 : neuron_cap;
+    if (!dense) S_AL(P.fired_list, int2, 2 * neuron_cap);
     S_AL(P.fired_count, int32_t, 2);
     S_AL(P.tables, float, table_cap);
     S_AL(P.groups, NcGroupDev, (int64_t)nets * kGroupsPerNet);
@@ -246,6 +268,8 @@ int nc_server::init(std::string& err)
     P.n_nets = nets;
     P.n_tiles = 0;
     P.n_tiles_dev = d_ntiles;
+    P.n_spans = 0;
+    P.n_spans_dev = d_nspans;
     a_neuron.reset(neuron_cap);
     a_ptr.reset(ptr_cap);
     a_word.reset(word_cap);
@@ -255,7 +279,8 @@ int nc_server::init(std::string& err)
     for (int32_t q = nets - 1; q >= 0; --q) free_slots.push_back(q);
     L.neuron_block = 256;
     L.launch_block = 256;
-    L.launch_blocks = std::max(1, sms * 4);
+    L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
+    L.dense_blocks = std::max(1, sms * NC_DENSE_MIN_BLOCKS);  // warps stride the tile table
     S_CK(cudaStreamSynchronize(stream));
     return capture(err);
 }
@@ -273,8 +298,13 @@ int nc_server::capture(std::string& err)
     NcPools Gg = G;
     Gg.n_tiles = (int32_t)std::min<int64_t>(G.n_tiles, nb_tiles);
     for (int k = 0; k < cfg.steps_per_batch && rc == 0; ++k) {
-        rc |= nc::launch_neuron_step(Gg, shape, stream);
-        rc |= nc::launch_spike_launch(G, shape, stream);
+        if (dense) {
+            rc |= nc::launch_dense_synapses(G, shape, stream);
+            rc |= nc::launch_dense_neurons(Gg, shape, stream);
+        } else {
+            rc |= nc::launch_neuron_step(Gg, shape, stream);
+            rc |= nc::launch_spike_launch(G, shape, stream);
+        }
     }
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -338,14 +368,14 @@ void nc_server::builder_loop()
         if (rc == NC_OK) {
             const nc::NetHost& h = r->host;
             r->syn_len = (h.s + 31) / 32 * 32;
-            r->ring_len = (int64_t)h.ring_slots * h.ring_words;
+            r->ring_len = dense ? 0 : (int64_t)h.ring_slots * h.ring_words;
             r->table_len = (int64_t)h.tables.size();
             r->words = (h.n + 31) / 32;
             if (h.n > neuron_cap || r->syn_len > syn_cap || r->ring_len > ring_cap || r->table_len > table_cap) {
                 rc = NC_ERR_BUDGET;
                 err = "network larger than the server's memory budget";
             }
-            r->bytes = (int64_t)(r->syn_len * kSynBytes + h.n * kNeuronBytes + r->ring_len * 4.0 + r->table_len * 4.0);
+            r->bytes = (int64_t)(r->syn_len * syn_bytes + h.n * kNeuronBytes + r->ring_len * 4.0 + r->table_len * 4.0);
         }
         r->status = rc;
         r->err = err;
@@ -399,17 +429,25 @@ int nc_server::admit(Resident& r, std::string& err)
     S_CK(put(P.orig_id, h.orig_id, nb, stream));
     S_CK(put(P.slot_of, h.slot_of, nb, stream));
     S_CK(put(P.in_ptr, inp, pb, stream));
-    S_CK(put(P.out_ptr, outp, pb, stream));
-    S_CK(put(P.ring_off, h.ring_off, pb, stream));
     S_CK(put(P.w, h.w, sb, stream));
     S_CK(put(P.inh, h.inh_bits, sb / 32, stream));
     S_CK(put(P.t_arr, never_s, sb, stream));
-    S_CK(put(P.last_arr, never_s, sb, stream));
-    S_CK(put(P.out_post, h.out_post, sb, stream));
-    S_CK(put(P.out_csc, h.out_csc, sb, stream));
-    S_CK(put(P.out_delay, h.out_delay, sb, stream));
-    S_CK(put(P.out_ringpos, h.out_ringpos, sb, stream));
-    S_CK(cudaMemsetAsync(P.ring + rb, 0, sizeof(uint32_t) * r.ring_len, stream));
+    if (dense) {
+        S_CK(put(P.csc_pre, h.csc_pre, sb, stream));
+        S_CK(put(P.csc_post, h.csc_post, sb, stream));
+        S_CK(put(P.csc_dl, h.csc_dl, sb, stream));
+        S_CK(put(P.la_c, never_s, sb, stream));
+        S_CK(cudaMemsetAsync(P.win + sb / 32, 0, sizeof(uint32_t) * (r.syn_len / 32), stream));
+    } else {
+        S_CK(put(P.out_ptr, outp, pb, stream));
+        S_CK(put(P.ring_off, h.ring_off, pb, stream));
+        S_CK(put(P.last_arr, never_s, sb, stream));
+        S_CK(put(P.out_post, h.out_post, sb, stream));
+        S_CK(put(P.out_csc, h.out_csc, sb, stream));
+        S_CK(put(P.out_delay, h.out_delay, sb, stream));
+        S_CK(put(P.out_ringpos, h.out_ringpos, sb, stream));
+        S_CK(cudaMemsetAsync(P.ring + rb, 0, sizeof(uint32_t) * r.ring_len, stream));
+    }
     for (int par = 0; par < 2; ++par) {
         S_CK(cudaMemsetAsync(P.fired + par * P.total_words + wb, 0, sizeof(uint32_t) * r.words, stream));
         S_CK(cudaMemsetAsync(P.forced + par * P.total_words + wb, 0, sizeof(uint32_t) * r.words, stream));
@@ -450,6 +488,7 @@ int nc_server::admit(Resident& r, std::string& err)
     d.pre_factor = h.p.presynaptic_factor;
     d.post_factor = h.p.postsynaptic_factor;
     d.e_term = h.e_term;
+    d.n_syn = h.s;
     d.stats = d_stats + 4 * (int64_t)r.slot;
     S_CK(cudaMemcpyAsync(P.nets + r.slot, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
     if (nc::launch_background_prologue(P, r.slot, h.n, stream)) {
@@ -489,6 +528,22 @@ int nc_server::upload_tiles(std::string& err)
     const int32_t n = (int32_t)tiles.size();
     if (n) S_CK(cudaMemcpyAsync(P.tiles, tiles.data(), tiles.size() * sizeof(NcTile), cudaMemcpyHostToDevice, stream));
     S_CK(cudaMemcpyAsync(d_ntiles, &n, sizeof(n), cudaMemcpyHostToDevice, stream));
+    std::vector<NcTile> spans;
+    if (dense) {
+        for (const auto& r : active) {
+            const int32_t chunks = (int32_t)((r->host.s + 31) / 32);
+            for (int32_t c = 0; c < chunks; c += NC_SPAN_CHUNKS) spans.push_back(NcTile{r->slot, c});
+        }
+        if ((int64_t)spans.size() > span_cap) {
+            err = "span table overflow";
+            return NC_ERR_INVALID;
+        }
+        const int32_t ns = (int32_t)spans.size();
+        if (ns)
+            S_CK(cudaMemcpyAsync(P.spans, spans.data(), spans.size() * sizeof(NcTile), cudaMemcpyHostToDevice, stream));
+        S_CK(cudaMemcpyAsync(d_nspans, &ns, sizeof(ns), cudaMemcpyHostToDevice, stream));
+        P.n_spans = ns;
+    }
     S_CK(cudaStreamSynchronize(stream));
     P.n_tiles = n;
     return NC_OK;
@@ -574,7 +629,8 @@ void nc_server::scheduler_loop()
         if (!done.empty()) {
             NcPools F = P;  // flush launched directly with the current tile count
             F.n_tiles_dev = nullptr;
-            if (nc::launch_stdp_flush(F, L, stream)) return;
+            F.n_spans_dev = nullptr;
+            if (dense ? nc::launch_flush_dense(F, L, stream) : nc::launch_stdp_flush(F, L, stream)) return;
             cudaStreamSynchronize(stream);
         }
         std::vector<nc_request_done> out;
@@ -641,7 +697,7 @@ int nc_server_create(const nc_server_config* config, nc_server** out)
     *out = nullptr;
     if (config->memory_budget_bytes <= 0 || config->max_networks < 1 || config->max_networks > 65536 ||
         config->steps_per_batch < 1 || config->steps_per_batch > 4096 || config->build_threads < 1 ||
-        config->build_threads > 256)
+        config->build_threads > 256 || (config->step_mode != NC_STEP_DENSE && config->step_mode != NC_STEP_EVENT))
         return sfail(NC_ERR_INVALID, "bad server configuration");
     int devices = 0;
     if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)

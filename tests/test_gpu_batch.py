@@ -7,6 +7,8 @@ from netgen import knn_net, random_net
 
 pytestmark = pytest.mark.gpu
 
+MODES = {"dense": 0, "event": 1}
+
 
 def mixed_nets(O=None, G=None):
     specs = []
@@ -24,9 +26,10 @@ def mixed_nets(O=None, G=None):
     return specs
 
 
-def batch_of(G, specs):
+def batch_of(G, specs, mode="dense"):
     return G.Batch([dict(xyz=s["xyz"], pre=s["pre"], post=s["post"], weight=s["weight"],
-                         params=G.default_params(**s["pkw"]), groups=s["groups"], horizon=s["horizon"])
+                         params=G.default_params(**s["pkw"], step_mode=MODES[mode]), groups=s["groups"],
+                         horizon=s["horizon"])
                     for s in specs])
 
 
@@ -44,21 +47,23 @@ def check_equal(b, q, o):
     assert st["steps"] == so["step"]
 
 
-def test_batch_each_net_as_alone(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_batch_each_net_as_alone(nc, oracle_mod, mode):
     specs = mixed_nets()
-    b = batch_of(nc, specs)
+    b = batch_of(nc, specs, mode)
     b.run_to_end()
     for q, s in enumerate(specs):
         assert b.step(q) == s["horizon"]
         check_equal(b, q, oracle_of(oracle_mod, s))
 
 
-def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod, mode):
     specs = mixed_nets()
-    b = batch_of(nc, specs)
-    shapes = [dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=0),
-              dict(neuron_block=256, launch_blocks=1216, launch_block=256, graph_steps=7),
-              dict(neuron_block=64, launch_blocks=3, launch_block=32, graph_steps=16)]
+    b = batch_of(nc, specs, mode)
+    shapes = [dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=0, dense_blocks=0),
+              dict(neuron_block=256, launch_blocks=1216, launch_block=256, graph_steps=7, dense_blocks=3),
+              dict(neuron_block=64, launch_blocks=3, launch_block=32, graph_steps=16, dense_blocks=304)]
     done = 0
     for k, sh in enumerate(shapes * 10):
         b.set_launch(**sh)
@@ -80,9 +85,10 @@ def test_batch_rejects_oversized_blocks(nc):
         b.set_launch(launch_block=48)
 
 
-def test_batch_autotune_keeps_results(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_batch_autotune_keeps_results(nc, oracle_mod, mode):
     specs = mixed_nets()
-    b = batch_of(nc, specs)
+    b = batch_of(nc, specs, mode)
     cfg = b.autotune(steps_per_trial=2)
     assert cfg["neuron_block"] % 32 == 0 and cfg["launch_blocks"] > 0
     b.run_to_end()

@@ -1,6 +1,8 @@
 """GPU step (libneucor_gb300.so through the C ABI) against the reference's own outputs
 (golden fixtures) and against the stepped CPU restatement (oracle), bit for bit:
-spike rasters, potentials, weights, activities, last-fire times and counters."""
+spike rasters, potentials, weights, activities, last-fire times and counters.  Every
+case runs in both forms of the step kernels (dense: one launch per step walking the
+in-rows; event: fired-list compaction and spike launch)."""
 import numpy as np
 import pytest
 
@@ -8,6 +10,8 @@ from netgen import knn_net, random_net
 from scenario import extra_by_step, groups_list, load, params_kw
 
 pytestmark = pytest.mark.gpu
+
+MODES = {"dense": 0, "event": 1}
 
 
 def bits(a):
@@ -59,12 +63,14 @@ def run_oracle_stepwise(o, steps, extras=None, checkpoints=()):
     return np.asarray(ras), np.asarray(pot_rows), weights
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("name", ["canonical_knn64", "canonical_random40_dt05", "canonical_knn100_nobg"])
-def test_gpu_matches_reference_fixture(nc, name):
+def test_gpu_matches_reference_fixture(nc, name, mode):
     """The GPU reproduces what the reference's own code computed, every step."""
     G = nc
     fx = load(name)
-    net = gpu_net(G, fx["xyz"], fx["pre"], fx["post"], fx["w"], params_kw(fx), groups_list(fx))
+    net = gpu_net(G, fx["xyz"], fx["pre"], fx["post"], fx["w"], dict(params_kw(fx), step_mode=MODES[mode]),
+                  groups_list(fx))
     np.testing.assert_array_equal(net.inhibitory(), fx["inhibitory"])
     steps = int(fx["steps"])
     ck = [int(c) for c in fx["checkpoints"]]
@@ -100,13 +106,14 @@ SCENARIOS = [
 ]
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("label,make,pkw,groups,steps", SCENARIOS, ids=[s[0] for s in SCENARIOS])
-def test_gpu_matches_oracle_stepwise(nc, oracle_mod, label, make, pkw, groups, steps):
+def test_gpu_matches_oracle_stepwise(nc, oracle_mod, label, make, pkw, groups, steps, mode):
     G, O = nc, oracle_mod
     xyz, pre, post, w = make()
     extras = {t: [(t * 37 + k * 11) % len(xyz) for k in range(3)] for t in range(2, steps, 13)}
     ck = (steps // 3, steps)
-    net = gpu_net(G, xyz, pre, post, w, pkw, groups)
+    net = gpu_net(G, xyz, pre, post, w, dict(pkw, step_mode=MODES[mode]), groups)
     o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw), groups=groups)
     np.testing.assert_array_equal(net.inhibitory(), o.inhibitory())
     np.testing.assert_array_equal(net.delays(), o.delays())
@@ -123,14 +130,15 @@ def test_gpu_matches_oracle_stepwise(nc, oracle_mod, label, make, pkw, groups, s
     assert so["fires"] > 0 and so["launched"] > 0
 
 
-def test_gpu_rate_changes_and_activity_reset(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_gpu_rate_changes_and_activity_reset(nc, oracle_mod, mode):
     """learningRate / factors changed between runs and resetActivities, as the renderer's
     sliders do (src/NeuCor_Renderer.cpp:1696-1712)."""
     G, O = nc, oracle_mod
     xyz, pre, post, w = knn_net(160, 12, 41)
     groups = [dict(first=0, count=16, rate_hz=40.0, correlated=1, jitter=2)]
     pkw = dict(seed=42)
-    net = gpu_net(G, xyz, pre, post, w, pkw, groups)
+    net = gpu_net(G, xyz, pre, post, w, dict(pkw, step_mode=MODES[mode]), groups)
     o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw), groups=groups)
     for lr, a, b in [(1.0, 0.13, 0.30), (0.0, 0.13, 0.30), (3.0, 0.05, 0.6), (1.0, 0.13, 0.30)]:
         net.learningRate, net.presynapticFactor, net.postsynapticFactor = lr, a, b
@@ -156,14 +164,15 @@ def c1_network(G, seed=1):
     return xyz, pre, post, w, groups
 
 
-def test_gpu_c1_full_horizon_bit_exact(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_gpu_c1_full_horizon_bit_exact(nc, oracle_mod, mode):
     """The 1k-neuron / 50k-synapse workload for its full 10,000 steps: every step's
     raster, and the final potentials, weights, activities and counters."""
     G, O = nc, oracle_mod
     xyz, pre, post, w, groups = c1_network(G)
     pkw = dict(seed=2024)
     steps = 10000
-    net = gpu_net(G, xyz, pre, post, w, pkw, groups)
+    net = gpu_net(G, xyz, pre, post, w, dict(pkw, step_mode=MODES[mode]), groups)
     net.record_raster(steps)
     net.run(steps)
     o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw), groups=groups)
@@ -176,7 +185,8 @@ def test_gpu_c1_full_horizon_bit_exact(nc, oracle_mod):
     assert (st["fires"], st["launched"], st["dropped"]) == (so["fires"], so["launched"], so["dropped"])
 
 
-def test_gpu_c2_prefix_bit_exact(nc, oracle_mod):
+@pytest.mark.parametrize("mode", MODES)
+def test_gpu_c2_prefix_bit_exact(nc, oracle_mod, mode):
     """The 100k-neuron / 10M-synapse workload (200 inputs in 10 groups at 5-40 Hz): the
     first 300 steps bit-exact against the oracle."""
     G, O = nc, oracle_mod
@@ -185,7 +195,7 @@ def test_gpu_c2_prefix_bit_exact(nc, oracle_mod):
     groups = [dict(first=20 * g, count=20, rate_hz=float(rates[g]), correlated=1, jitter=2) for g in range(10)]
     pkw = dict(seed=99)
     steps = 300
-    net = gpu_net(G, xyz, pre, post, w, pkw, groups)
+    net = gpu_net(G, xyz, pre, post, w, dict(pkw, step_mode=MODES[mode]), groups)
     net.record_raster(steps)
     net.run(steps)
     o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw), groups=groups)

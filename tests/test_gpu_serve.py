@@ -24,10 +24,12 @@ def requests():
     return out
 
 
-def test_served_results_equal_alone(nc, oracle_mod):
+@pytest.mark.parametrize("mode", [0, 1], ids=["dense", "event"])
+def test_served_results_equal_alone(nc, oracle_mod, mode):
     G, O = nc, oracle_mod
     reqs = requests()
-    srv = G.Server(budget_bytes=256 << 20, max_networks=3, steps_per_batch=16, build_threads=4, keep_results=True)
+    srv = G.Server(budget_bytes=256 << 20, max_networks=3, steps_per_batch=16, build_threads=4, keep_results=True,
+                   step_mode=mode)
     ids = []
     for q, r in enumerate(reqs):
         ids.append(srv.submit(dict(xyz=r["xyz"], pre=r["pre"], post=r["post"], weight=r["weight"],

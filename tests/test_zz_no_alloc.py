@@ -2,9 +2,10 @@
 network is set up (code recording the step into its own CUDA graph, where allocation is
 not allowed during stream capture; services with a fixed device-memory budget).
 
-It launches the same kernels as nc_run with their per-step scratch in a static device
-array, so it must compute exactly what nc_run computes; checked on two calls in a row,
-bit for bit (the tolerance of every parity test here), through the C ABI."""
+It launches the same kernels as nc_run (the event form with its per-step scratch in a
+static device array; the dense form needs none), so it must compute exactly what nc_run
+computes; checked on two calls in a row in both forms, bit for bit (the tolerance of
+every parity test here), through the C ABI."""
 import ctypes
 
 import numpy as np
@@ -23,13 +24,13 @@ def noalloc_fn(G):
     return fn, L
 
 
-def make_pair(G):
+def make_pair(G, mode):
     xyz, pre, post, w = knn_net(2500, 12, 77, inhibitory=0.1)
     groups = [dict(first=0, count=25, rate_hz=30.0, correlated=1, jitter=2),
               dict(first=25, count=25, rate_hz=30.0, correlated=0)]
     nets = []
     for _ in range(2):
-        net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(seed=4242))
+        net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(seed=4242, step_mode=mode))
         net.set_input_groups(groups)
         nets.append(net)
     return nets
@@ -39,9 +40,10 @@ def bits(a):
     return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
 
 
-def test_noalloc_matches_run_on_two_calls(nc):
+@pytest.mark.parametrize("mode", [0, 1], ids=["dense", "event"])
+def test_noalloc_matches_run_on_two_calls(nc, mode):
     run_noalloc, L = noalloc_fn(nc)
-    ref, na = make_pair(nc)
+    ref, na = make_pair(nc, mode)
     for call in range(2):
         ref.record_raster(120)
         na.record_raster(120)
@@ -59,11 +61,11 @@ def test_noalloc_matches_run_on_two_calls(nc):
         assert na.step == ref.step == 120 * (call + 1)
 
 
-def test_noalloc_refuses_networks_above_its_limit(nc):
+def test_noalloc_refuses_event_networks_above_its_limit(nc):
     run_noalloc, L = noalloc_fn(nc)
     limit = 262144
     xyz, pre, post, w = nc.build_knn(limit + 1, 2, 8.0, seed=3)
-    big = nc.NeuCor.from_arrays(xyz, pre, post, w)
+    big = nc.NeuCor.from_arrays(xyz, pre, post, w, params=nc.default_params(step_mode=1))
     rc = run_noalloc(big._handle(), 1, None)
     assert rc == -1
     assert str(limit) in L.nc_last_error().decode()
