@@ -46,7 +46,7 @@ constexpr int kQueue = 64;                // launched-term queue per warp
 static_assert(NC_SPAN_CHUNKS % kUnroll == 0, "span chunks must be a multiple of the unroll");
 
 struct SynShared {
-    int64_t qs[kMaxWarps][kQueue];  // pool index of the launched synapse
+    int32_t qs[kMaxWarps][kQueue];  // launched synapse, relative to its span's first
     float qx[kMaxWarps][kQueue];    // deltaT * AP_depolFac of the launch
 };
 
@@ -59,12 +59,123 @@ __device__ __forceinline__ int warp_sum(int v)
 
 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT) for the queued launches [0, count)
 // (src/NeuCor.cpp:695); lane l takes entry l.
-__device__ __forceinline__ void drain_terms(const NcPools& P, const NcNetDesc& D, SynShared& sh, int wib, int lane,
+__device__ __forceinline__ void drain_terms(double* term_span, double e_term, SynShared& sh, int wib, int lane,
                                             int count)
 {
     __syncwarp();
-    if (lane < count) P.term[sh.qs[wib][lane]] = __dmul_rn(__dmul_rn((double)sh.qx[wib][lane], 0.9943), D.e_term);
+    if (lane < count) term_span[sh.qs[wib][lane]] = __dmul_rn(__dmul_rn((double)sh.qx[wib][lane], 0.9943), e_term);
     __syncwarp();
+}
+
+// Synapse::fire and the deferred plasticity of step `prev` for the span's chunks (see
+// k_dense_synapses); kAll: every chunk of the span lies inside the net.
+template <bool kAll>
+__device__ __forceinline__ void span_chunks(const NcPools& P, const NcNetDesc& D, SynShared& sh, int wib, int lane,
+                                            int64_t s_span, int32_t rem, int32_t t, int32_t prev, int& qn, int& nl,
+                                            int& nd)
+{
+    const int32_t kc = D.kc;
+    const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
+    const int32_t* lfn = P.lf + D.neuron_base;
+    const float* tab_pre = P.tables + D.table_base;
+    const float* tab_post = tab_pre + D.tab_pre_len;
+    // this lane's synapse in the span's first chunk, in every stream
+    const int32_t* pre_p = P.csc_pre + s_span + lane;
+    const int32_t* post_p = P.csc_post + s_span + lane;
+    const uint16_t* dl_p = P.csc_dl + s_span + lane;
+    int32_t* la_p = P.la_c + s_span + lane;
+    float* w_p = P.w + s_span + lane;
+    int32_t* ta_p = P.t_arr + s_span + lane;
+    const uint32_t* inh_p = P.inh + (s_span >> 5);
+    uint32_t* win_p = P.win + (s_span >> 5);
+    double* term_span = P.term + s_span;
+    const float dt = D.dt, c52 = D.c52;
+    for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
+        int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
+        uint32_t dl[kUnroll], fword[kUnroll], ihw[kUnroll];
+        float wv[kUnroll];
+        bool in[kUnroll];
+        // every load of the pass is issued before the first use
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int q = (h + u) * 32;
+            in[u] = kAll || q < rem;
+            if (in[u]) {
+                pre[u] = __ldg(pre_p + q);
+                post[u] = __ldg(post_p + q);
+                dl[u] = __ldg(dl_p + q);
+                la[u] = la_p[q];
+                wv[u] = w_p[q];
+                ta[u] = ta_p[q];
+                ihw[u] = __ldg(inh_p + h + u);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (in[u]) {
+                fword[u] = fprev[pre[u] >> 5];
+                lfp[u] = lfn[post[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int q = (h + u) * 32;
+            int32_t lac = NC_NEVER;
+            bool launch = false;
+            float x = 0.0f;
+            if (in[u]) {
+                lac = la[u];
+                const bool tf = lfp[u] == prev;  // target fired at prev
+                const bool srcf = (fword[u] >> (pre[u] & 31)) & 1u;
+                const bool arrived = la[u] == prev;
+                const int32_t after = (int32_t)((dl[u] >> 14) & 1u);
+                launch = srcf && (la[u] == NC_NEVER || prev - la[u] >= kc + after);
+                nl += launch;
+                nd += srcf && !launch;
+                const bool ih = (ihw[u] >> lane) & 1u;
+                const float w0 = wv[u];
+                float w1 = w0;
+                if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
+                if (launch) {
+                    // target below the source in caller order and fired at prev: its
+                    // update ran first, post-spike plasticity included
+                    const float cap = (((dl[u] >> 15) & 1u) && tf) ? w1 : w0;
+                    // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                    x = dt * (c52 * cap);
+                    lac = prev + (int32_t)(dl[u] & 0x3fffu);
+                    la_p[q] = lac;
+                }
+                float w2 = w1;
+                if (arrived) {
+                    w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
+                    ta_p[q] = prev;
+                }
+                if (tf || arrived) w_p[q] = w2;
+            }
+            // arrived t-KC .. t-1: in the fold of step t
+            const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
+            const uint32_t wm = __ballot_sync(kFull, win);
+            if (lane == 0 && (kAll || q < rem + lane)) win_p[h + u] = wm;
+            const uint32_t lm = __ballot_sync(kFull, launch);
+            if (lm) {
+                if (launch) {
+                    const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                    sh.qs[wib][pos] = q + lane;
+                    sh.qx[wib][pos] = x;
+                }
+                qn += __popc(lm);
+                if (qn >= 32) {
+                    drain_terms(term_span, D.e_term, sh, wib, lane, 32);
+                    if (lane < qn - 32) {
+                        sh.qs[wib][lane] = sh.qs[wib][32 + lane];
+                        sh.qx[wib][lane] = sh.qx[wib][32 + lane];
+                    }
+                    __syncwarp();
+                    qn -= 32;
+                }
+            }
+        }
+    }
 }
 
 // Adds each warp's per-net counters (K of them, into stats[first ..]) to the nets'
@@ -133,108 +244,256 @@ __global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses(NcP
             acc_net = span.net;
             acc[0] = acc[1] = 0;
         }
-        const int64_t sb = D.syn_base;
-        const int64_t nsyn = D.n_syn;
-        const int32_t kc = D.kc;
-        const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
-        const int32_t* lfn = P.lf + D.neuron_base;
-        const float* tab_pre = P.tables + D.table_base;
-        const float* tab_post = tab_pre + D.tab_pre_len;
+        const int64_t s_span = D.syn_base + (int64_t)span.first * 32;
+        // synapses of the span inside the net, counted from this lane's first one
+        const int64_t rem64 = D.n_syn - (int64_t)span.first * 32 - lane;
         int qn = 0, nl = 0, nd = 0;
-        for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
-            int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
-            uint32_t dl[kUnroll], fword[kUnroll], ihw[kUnroll];
-            float wv[kUnroll];
-            bool in[kUnroll];
-            // every load of the pass is issued before the first use
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const int64_t c = span.first + h + u;
-                const int64_t rel = c * 32 + lane;
-                in[u] = rel < nsyn;
-                ihw[u] = 0u;
-                if (in[u]) {
-                    const int64_t s = sb + rel;
-                    pre[u] = __ldg(P.csc_pre + s);
-                    post[u] = __ldg(P.csc_post + s);
-                    dl[u] = __ldg(P.csc_dl + s);
-                    la[u] = P.la_c[s];
-                    wv[u] = P.w[s];
-                    ta[u] = P.t_arr[s];
-                    ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                fword[u] = 0u;
-                lfp[u] = NC_NEVER;
-                if (in[u]) {
-                    fword[u] = fprev[pre[u] >> 5];
-                    lfp[u] = lfn[post[u]];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const int64_t c = span.first + h + u;
-                const int64_t s = sb + c * 32 + lane;
-                int32_t lac = in[u] ? la[u] : NC_NEVER;
-                bool launch = false;
-                float x = 0.0f;
-                if (in[u]) {
-                    const bool tf = lfp[u] == prev;  // target fired at prev
-                    const bool srcf = (fword[u] >> (pre[u] & 31)) & 1u;
-                    const bool arrived = la[u] == prev;
-                    const int32_t after = (int32_t)((dl[u] >> 14) & 1u);
-                    launch = srcf && (la[u] == NC_NEVER || prev - la[u] >= kc + after);
-                    nl += launch;
-                    nd += srcf && !launch;
-                    const bool ih = (ihw[u] >> lane) & 1u;
-                    const float w0 = wv[u];
-                    float w1 = w0;
-                    if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
-                    if (launch) {
-                        // target below the source in caller order and fired at prev: its
-                        // update ran first, post-spike plasticity included
-                        const float cap = (((dl[u] >> 15) & 1u) && tf) ? w1 : w0;
-                        // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                        x = D.dt * (D.c52 * cap);
-                        lac = prev + (int32_t)(dl[u] & 0x3fffu);
-                        P.la_c[s] = lac;
-                    }
-                    float w2 = w1;
-                    if (arrived) {
-                        w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
-                        P.t_arr[s] = prev;
-                    }
-                    if (tf || arrived) P.w[s] = w2;
-                }
-                // arrived t-KC .. t-1: in the fold of step t
-                const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
-                const uint32_t wm = __ballot_sync(kFull, win);
-                if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
-                const uint32_t lm = __ballot_sync(kFull, launch);
-                if (lm) {
-                    if (launch) {
-                        const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                        sh.qs[wib][pos] = s;
-                        sh.qx[wib][pos] = x;
-                    }
-                    qn += __popc(lm);
-                    if (qn >= 32) {
-                        drain_terms(P, D, sh, wib, lane, 32);
-                        if (lane < qn - 32) {
-                            sh.qs[wib][lane] = sh.qs[wib][32 + lane];
-                            sh.qx[wib][lane] = sh.qx[wib][32 + lane];
-                        }
-                        __syncwarp();
-                        qn -= 32;
-                    }
-                }
-            }
-        }
-        if (qn > 0) drain_terms(P, D, sh, wib, lane, qn);
+        if (D.n_syn - (int64_t)span.first * 32 >= NC_SPAN_CHUNKS * 32)
+            span_chunks<true>(P, D, sh, wib, lane, s_span, 0, t, prev, qn, nl, nd);
+        else
+            span_chunks<false>(P, D, sh, wib, lane, s_span, (int32_t)rem64, t, prev, qn, nl, nd);
+        if (qn > 0) drain_terms(P.term + s_span, D.e_term, sh, wib, lane, qn);
         acc[0] += (unsigned long long)warp_sum(nl);
         acc[1] += (unsigned long long)warp_sum(nd);
+    }
+    block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
+}
+
+// ---------------------------------------------------------------- staged synapse pass
+// The same pass with the span's six in-synapse streams staged into shared memory by the
+// bulk-copy (TMA) engine: each warp keeps the next span's copies in flight while it
+// works on the current one, so the memory system sees ~11 KB per warp outstanding
+// instead of the few loads a warp's registers can hold.
+
+constexpr int kStageWarps = 4;  // 128-thread blocks
+constexpr int kSpanSyn = NC_SPAN_CHUNKS * 32;
+
+struct StageBuf {                 // one span, as laid out in the pools (16-byte multiples)
+    int32_t pre[kSpanSyn];
+    int32_t post[kSpanSyn];
+    int32_t la[kSpanSyn];
+    float w[kSpanSyn];
+    int32_t ta[kSpanSyn];
+    uint16_t dl[kSpanSyn];
+};
+
+struct WarpStage {
+    StageBuf buf[2];
+    unsigned long long bar[2];    // mbarriers: the copies of buf[k] have landed
+    int64_t qs[kQueue];
+    float qx[kQueue];
+};
+
+constexpr size_t kStageSmem = sizeof(WarpStage) * kStageWarps;
+constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait polls before a stage gives up
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// Lane 0: copies span `sp` into b (all six streams), completing on *bar.  Returns 0
+// when the span's net is skipped this launch (nothing copied).
+__device__ int stage_span(const NcPools& P, int sp, bool flush, StageBuf* b, unsigned long long* bar)
+{
+    const NcTile span = P.spans[sp];
+    const NcNetDesc& D = P.nets[span.net];
+    const int32_t t = D.t, prev = t - 1;
+    if (!D.active || prev < 1 || D.stdp_done >= prev || (!flush && t > D.t_end)) return 0;
+    const int64_t chunks = (D.n_syn + 31) / 32;
+    const int64_t nch = min((int64_t)NC_SPAN_CHUNKS, chunks - span.first);
+    const int64_t s = D.syn_base + (int64_t)span.first * 32;
+    const uint32_t b4 = (uint32_t)(nch * 128), b2 = (uint32_t)(nch * 64);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)), "r"(5 * b4 + b2)
+                 : "memory");
+    bulk_copy(b->pre, P.csc_pre + s, b4, bar);
+    bulk_copy(b->post, P.csc_post + s, b4, bar);
+    bulk_copy(b->la, P.la_c + s, b4, bar);
+    bulk_copy(b->w, P.w + s, b4, bar);
+    bulk_copy(b->ta, P.t_arr + s, b4, bar);
+    bulk_copy(b->dl, P.csc_dl + s, b2, bar);
+    return 1;
+}
+
+// All lanes: bounded wait for the phase of *bar.
+__device__ __forceinline__ bool stage_wait(unsigned long long* bar, uint32_t phase)
+{
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(a), "r"(phase) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <bool kFlush>
+__global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(NcPools P)
+{
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    __shared__ int s_net[kStageWarps];
+    __shared__ unsigned long long s_acc[kStageWarps][2];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kStageWarps + wib;
+    const int nw = gridDim.x * kStageWarps;
+    const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
+    WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[wib];
+
+    if (lane == 0) {
+        for (int k = 0; k < 2; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&ws.bar[k])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+
+    int acc_net = -1;
+    unsigned long long acc[2] = {0, 0};  // launched, dropped
+    uint32_t phases = 0u;  // bit k: parity of buf[k]'s next completion
+    int cur = 0;
+    int issued = 0;  // lane 0's answer for the buffer `cur`, broadcast below
+    if (gw < n_spans && lane == 0) issued = stage_span(P, gw, kFlush, &ws.buf[0], &ws.bar[0]);
+    bool ok = true;
+    for (int sp = gw; sp < n_spans && ok; sp += nw) {
+        const int nxt = sp + nw;
+        int issued_next = 0;
+        if (nxt < n_spans && lane == 0) issued_next = stage_span(P, nxt, kFlush, &ws.buf[cur ^ 1], &ws.bar[cur ^ 1]);
+        const int this_issued = __shfl_sync(kFull, issued, 0);
+        issued = issued_next;
+        if (this_issued) {
+            if (!stage_wait(&ws.bar[cur], (phases >> cur) & 1u)) {
+                if (lane == 0) atomicOr(P.dev_err, NC_DEV_ERR_STAGE_TIMEOUT);
+                ok = false;
+                break;
+            }
+            phases ^= 1u << cur;
+            const StageBuf& B = ws.buf[cur];
+            const NcTile span = P.spans[sp];
+            const NcNetDesc& D = P.nets[span.net];
+            const int32_t t = D.t;
+            const int32_t prev = t - 1;
+            if (span.net != acc_net) {
+                if (acc_net >= 0 && lane == 0) {
+                    unsigned long long* st = P.nets[acc_net].stats;
+                    atomicAdd(st + 1, acc[0]);
+                    atomicAdd(st + 2, acc[1]);
+                }
+                acc_net = span.net;
+                acc[0] = acc[1] = 0;
+            }
+            const int64_t sb = D.syn_base;
+            const int64_t nsyn = D.n_syn;
+            const int32_t kc = D.kc;
+            const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
+            const int32_t* lfn = P.lf + D.neuron_base;
+            const float* tab_pre = P.tables + D.table_base;
+            const float* tab_post = tab_pre + D.tab_pre_len;
+            int qn = 0, nl = 0, nd = 0;
+            for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
+                uint32_t fword[kUnroll], ihw[kUnroll];
+                int32_t lfp[kUnroll];
+                bool in[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int64_t c = span.first + h + u;
+                    const int q = (h + u) * 32 + lane;
+                    in[u] = c * 32 + lane < nsyn;
+                    fword[u] = 0u;
+                    lfp[u] = NC_NEVER;
+                    ihw[u] = 0u;
+                    if (in[u]) {
+                        fword[u] = fprev[B.pre[q] >> 5];
+                        lfp[u] = lfn[B.post[q]];
+                        ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int64_t c = span.first + h + u;
+                    const int q = (h + u) * 32 + lane;
+                    const int64_t s = sb + c * 32 + lane;
+                    const int32_t la = B.la[q];
+                    int32_t lac = in[u] ? la : NC_NEVER;
+                    bool launch = false;
+                    float x = 0.0f;
+                    if (in[u]) {
+                        const uint32_t dl = B.dl[q];
+                        const bool tf = lfp[u] == prev;  // target fired at prev
+                        const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
+                        const bool arrived = la == prev;
+                        const int32_t after = (int32_t)((dl >> 14) & 1u);
+                        launch = srcf && (la == NC_NEVER || prev - la >= kc + after);
+                        nl += launch;
+                        nd += srcf && !launch;
+                        const bool ih = (ihw[u] >> lane) & 1u;
+                        const float w0 = B.w[q];
+                        float w1 = w0;
+                        if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, B.ta[q]), 0.0f, D);
+                        if (launch) {
+                            // target below the source in caller order and fired at prev:
+                            // its update ran first, post-spike plasticity included
+                            const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
+                            // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                            x = D.dt * (D.c52 * cap);
+                            lac = prev + (int32_t)(dl & 0x3fffu);
+                            P.la_c[s] = lac;
+                        }
+                        float w2 = w1;
+                        if (arrived) {
+                            w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
+                            P.t_arr[s] = prev;
+                        }
+                        if (tf || arrived) P.w[s] = w2;
+                    }
+                    // arrived t-KC .. t-1: in the fold of step t
+                    const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
+                    const uint32_t wm = __ballot_sync(kFull, win);
+                    if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
+                    const uint32_t lm = __ballot_sync(kFull, launch);
+                    if (lm) {
+                        if (launch) {
+                            const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                            ws.qs[pos] = s;
+                            ws.qx[pos] = x;
+                        }
+                        qn += __popc(lm);
+                        if (qn >= 32) {
+                            __syncwarp();
+                            P.term[ws.qs[lane]] = __dmul_rn(__dmul_rn((double)ws.qx[lane], 0.9943), D.e_term);
+                            __syncwarp();
+                            if (lane < qn - 32) {
+                                ws.qs[lane] = ws.qs[32 + lane];
+                                ws.qx[lane] = ws.qx[32 + lane];
+                            }
+                            __syncwarp();
+                            qn -= 32;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane < qn) P.term[ws.qs[lane]] = __dmul_rn(__dmul_rn((double)ws.qx[lane], 0.9943), D.e_term);
+            acc[0] += (unsigned long long)warp_sum(nl);
+            acc[1] += (unsigned long long)warp_sum(nd);
+        }
+        // the buffer is refilled by the next iteration's copy: finish reading it first,
+        // and order those reads before the copy engine's writes
+        __syncwarp();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        cur ^= 1;
+    }
+    if (!ok) {
+        // let this warp's copies in flight land (bounded) before the block's shared
+        // memory goes away: the one that timed out and the prefetch behind it
+        stage_wait(&ws.bar[cur], (phases >> cur) & 1u);
+        if (__shfl_sync(kFull, issued, 0)) stage_wait(&ws.bar[cur ^ 1], (phases >> (cur ^ 1)) & 1u);
     }
     block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
 }
@@ -282,25 +541,44 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
             if (s1 > s0) {
                 double pd = (double)pot;
                 const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
-                for (int64_t wa = wa0; wa <= wa1; wa += 2) {
-                    uint32_t x = P.win[wa];
-                    if (wa == wa0) x &= ~0u << (s0 & 31);
-                    if (wa == wa1 && (s1 & 31)) x &= (1u << (s1 & 31)) - 1u;
-                    uint32_t y = 0u;
-                    if (wa + 1 <= wa1) {
-                        y = P.win[wa + 1];
-                        if (wa + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
+                // the row's window bits, 256 synapses (8 words) at a time, streamed in
+                // batches of 8 across word boundaries so that a warp's batch count is
+                // its busiest lane's, not a sum of per-word maxima
+                for (int64_t wb = wa0; wb <= wa1; wb += 8) {
+                    unsigned long long m[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int64_t wq = wb + 2 * q;
+                        uint32_t x = wq <= wa1 ? P.win[wq] : 0u;
+                        uint32_t y = wq + 1 <= wa1 ? P.win[wq + 1] : 0u;
+                        if (wq == wa0) x &= ~0u << (s0 & 31);
+                        if (wq == wa1 && (s1 & 31)) x &= (1u << (s1 & 31)) - 1u;
+                        if (wq + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
+                        m[q] = x | ((unsigned long long)y << 32);
                     }
-                    unsigned long long bits = x | ((unsigned long long)y << 32);
-                    const double* tp = P.term + wa * 32;
-                    while (bits) {
+                    const double* tp = P.term + wb * 32;
+                    unsigned long long m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
+                    int base = 0;
+                    while (m0 | m1 | m2 | m3) {
                         int b[8];
-                        pop8_64(&bits, b);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            // on to the next pair when this one is spent (an empty pair costs a slot)
+                            if (m0 == 0ull) {
+                                m0 = m1;
+                                m1 = m2;
+                                m2 = m3;
+                                m3 = 0ull;
+                                base += 64;
+                            }
+                            b[k] = m0 ? base + __ffsll((long long)m0) - 1 : -1;
+                            m0 &= m0 - 1ull;
+                        }
                         double v[8];
 #pragma unroll
                         for (int k = 0; k < 8; ++k)
                             if (b[k] >= 0) v[k] = tp[b[k]];
-                        pd = fold8(pd, v, b);
+                        pd = fold8(pd, v, b, tp);
                     }
                 }
                 pot = __double2float_rn(pd);
@@ -368,9 +646,35 @@ __global__ void k_dense_mark_flushed(NcPools P)
     }
 }
 
+#ifndef NC_DENSE_STAGED
+#define NC_DENSE_STAGED 0
+#endif
+
 int syn_blocks(const NcPools& P, const nc::LaunchShape& L)
 {
-    return L.dense_blocks > 0 ? L.dense_blocks : (P.n_spans + kMaxWarps - 1) / kMaxWarps;
+    const int wpb = NC_DENSE_STAGED ? kStageWarps : kMaxWarps;
+    return L.dense_blocks > 0 ? L.dense_blocks : (P.n_spans + wpb - 1) / wpb;
+}
+
+template <bool kFlush>
+int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
+{
+    const int blocks = syn_blocks(P, L);
+    if (blocks <= 0) return 0;
+    if (NC_DENSE_STAGED) {
+        static bool attr_set[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+            cudaFuncSetAttribute(k_dense_synapses_staged<kFlush>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kStageSmem);
+            attr_set[dev] = true;
+        }
+        k_dense_synapses_staged<kFlush><<<blocks, 32 * kStageWarps, kStageSmem, s>>>(P);
+    } else {
+        k_dense_synapses<kFlush><<<blocks, 32 * kMaxWarps, 0, s>>>(P);
+    }
+    return 0;
 }
 
 }  // namespace
@@ -379,8 +683,7 @@ namespace nc {
 
 int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    const int blocks = syn_blocks(P, L);
-    if (blocks > 0) k_dense_synapses<false><<<blocks, 32 * kMaxWarps, 0, (cudaStream_t)stream>>>(P);
+    launch_syn<false>(P, L, (cudaStream_t)stream);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -399,8 +702,7 @@ int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream)
 
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    const int blocks = syn_blocks(P, L);
-    if (blocks > 0) k_dense_synapses<true><<<blocks, 32 * kMaxWarps, 0, (cudaStream_t)stream>>>(P);
+    launch_syn<true>(P, L, (cudaStream_t)stream);
     k_dense_mark_flushed<<<1, 256, 0, (cudaStream_t)stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

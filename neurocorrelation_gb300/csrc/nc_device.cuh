@@ -60,20 +60,28 @@ static __device__ __forceinline__ double rn32_int(double d, bool& rare)
     return __longlong_as_double((long long)u);
 }
 
-// Folds v[k] for every k with b[k] >= 0, in k order, into the float-valued pd.
-static __device__ __forceinline__ double fold8(double pd, const double v[8], const int b[8])
+// Exact `float += double` of the terms tp[b_k] (b_k >= 0, in k order) with the
+// hardware conversion.  Kept out of line so that the rare redo below is a branch and
+// its conversions are not issued with every batch.
+static __device__ __noinline__ double fold_exact8(double pd, const double* tp, int b0, int b1, int b2, int b3, int b4,
+                                                  int b5, int b6, int b7)
+{
+    const int b[8] = {b0, b1, b2, b3, b4, b5, b6, b7};
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (b[k] >= 0) pd = (double)__double2float_rn(__dadd_rn(pd, tp[b[k]]));
+    return pd;
+}
+
+// Folds v[k] = tp[b[k]] for every k with b[k] >= 0 (ascending), into the float-valued pd.
+static __device__ __forceinline__ double fold8(double pd, const double v[8], const int b[8], const double* tp)
 {
     const double pd0 = pd;
     bool rare = false;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (b[k] >= 0) pd = rn32_int(__dadd_rn(pd, v[k]), rare);
-    if (__builtin_expect(rare, 0)) {
-        pd = pd0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (b[k] >= 0) pd = (double)__double2float_rn(__dadd_rn(pd, v[k]));
-    }
+    if (__builtin_expect(rare, 0)) pd = fold_exact8(pd0, tp, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7]);
     return pd;
 }
 

@@ -34,6 +34,9 @@
 
 #define NC_NEVER INT32_MIN
 
+// Device error codes (NcPools::dev_err).
+#define NC_DEV_ERR_STAGE_TIMEOUT 1u  // a bulk copy into shared memory did not complete in time
+
 // Draw streams (third Philox counter word).
 #define NC_STREAM_BACKGROUND 1u
 #define NC_STREAM_SOURCE 2u
@@ -144,6 +147,7 @@ struct NcPools {
     // engine
     int32_t* tick;       // engine tick (parity of the fired list)
     uint32_t* done_ctr;  // last-block detection
+    uint32_t* dev_err;   // nonzero: a bounded device wait gave up (NC_DEV_ERR_*)
 };
 
 // ------------------------------------------------------------------ Philox

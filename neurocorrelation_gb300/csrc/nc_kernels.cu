@@ -218,10 +218,11 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             int b[8];
                             pop8_64(&bits, b);
                             double v[8];
+                            const double* tp = P.term + sb;
 #pragma unroll
                             for (int k = 0; k < 8; ++k)
-                                if (b[k] >= 0) v[k] = P.term[sb + b[k]];
-                            pd = fold8(pd, v, b);
+                                if (b[k] >= 0) v[k] = tp[b[k]];
+                            pd = fold8(pd, v, b, tp);
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
                         if (oldest >= 1) {

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
+#include <string>
 
 namespace nc {
 
@@ -209,6 +210,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(P.tiles, NcTile, tiles);
     NC_ALLOC(P.tick, int32_t, 1);
     NC_ALLOC(P.done_ctr, uint32_t, 1);
+    NC_ALLOC(P.dev_err, uint32_t, 1);
     NC_ALLOC(d_stats_, unsigned long long, 4 * nets.size());
     P.n_nets = (int32_t)nets.size();
     P.n_tiles = (int32_t)tiles;
@@ -390,6 +392,12 @@ int Engine::flush_plasticity(std::string& err)
 int Engine::sync(std::string& err)
 {
     NC_CK(cudaStreamSynchronize(stream));
+    uint32_t dev_err = 0;
+    NC_CK(cudaMemcpy(&dev_err, P.dev_err, sizeof(dev_err), cudaMemcpyDeviceToHost));
+    if (dev_err) {
+        err = "a device wait gave up (code " + std::to_string(dev_err) + ")";
+        return NC_ERR_TIMEOUT;
+    }
     return NC_OK;
 }
 

@@ -262,6 +262,7 @@ int nc_server::init(std::string& err)
     S_AL(P.tiles, NcTile, tile_cap);
     S_AL(P.tick, int32_t, 1);
     S_AL(P.done_ctr, uint32_t, 1);
+    S_AL(P.dev_err, uint32_t, 1);
     S_AL(d_stats, unsigned long long, 4 * (int64_t)nets);
     S_AL(d_ntiles, int32_t, 1);
 #undef S_AL
