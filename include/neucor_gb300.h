@@ -151,11 +151,32 @@ int nc_destroy(nc_net* net);
 /* Poisson input groups (replaces the role of NeuCor::setInputRateArray,
  * src/NeuCor.cpp:46-64, with the correlated trains of the benchmark workloads). */
 int nc_set_input_groups(nc_net* net, int32_t n_groups, const nc_group* groups);
-/* Periodic input firers with the reference's rates, positions and radii
- * (NeuCor::setInputRateArray + InputFirer, src/NeuCor.cpp:46-64, 305-345) —
- * not implemented in the stepped model yet. */
+/* Periodic input firers (NeuCor::setInputRateArray, src/NeuCor.cpp:46-64, and
+ * InputFirer, src/NeuCor.cpp:305-345).  Firers are appended or removed from the end to
+ * match `count`; the i-th appended firer sits at xyz[3i..3i+2] with radius[i] (both
+ * NULL: a random position from the C library's rand(), as the reference, and radius
+ * 1).  rates_hz[i] is firer i's frequency (the reference re-reads its borrowed array
+ * every run; here the rates are copied: change them with nc_set_input_rates).  Each
+ * firer keeps the reference's schedule (lastFire + k*1000/f, float/double arithmetic);
+ * a fire time in (t*dt, (t+1)*dt) fires every neuron closer than the radius at step
+ * t+1 with Neuron::fire's semantics (no threshold or refractory test).  Like the
+ * reference, a period of a whole number of steps never fires unless shifted with
+ * nc_add_input_offset.  Every change evaluates the interval after the last completed
+ * step at once. */
 int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
                             const float* radius);
+/* New frequencies of the first `count` firers (the reference's borrowed rate array). */
+int nc_set_input_rates(nc_net* net, int32_t count, const float* rates_hz);
+/* NeuCor::addInputOffset (src/NeuCor.cpp:66-68): shifts firer `id`'s lastFire by t ms. */
+int nc_add_input_offset(nc_net* net, int32_t id, float t_ms);
+/* NeuCor::setDetectors (src/NeuCor.cpp:70-77): appends `count` voltage detectors at
+ * xyz[3i..] with radius[i] (NULL: random positions from rand(), radius 1). */
+int nc_set_detectors(nc_net* net, int32_t count, const float* xyz, const float* radius);
+/* NeuCor::getDetectorVoltages / getDetectorVoltage (src/NeuCor.cpp:79-87, 359-366): the
+ * mean potential of each detector's neurons (float sum in id order; NaN with no neuron
+ * in range), as of the last completed step.  *count receives the detector count. */
+int nc_get_detector_voltages(nc_net* net, float* out, int32_t capacity, int32_t* count);
+int nc_get_detector_voltage(nc_net* net, int32_t id, float* out);
 /* Runtime-settable rates (NeuCor::learningRate, presynapticFactor,
  * postsynapticFactor are read live by the reference, src/NeuCor.cpp:757-758). */
 int nc_set_rates(nc_net* net, float learning_rate, float presynaptic_factor, float postsynaptic_factor);

@@ -99,6 +99,8 @@ public:
             presynapticFactor = o.presynapticFactor; postsynapticFactor = o.postsynapticFactor; seed = o.seed;
             xyz_ = std::move(o.xyz_); from_ = std::move(o.from_); to_ = std::move(o.to_); w_ = std::move(o.w_);
             groups_ = std::move(o.groups_);
+            inputArray_ = o.inputArray_;
+            inputRates_ = std::move(o.inputRates_);
             net_ = o.net_;
             o.net_ = nullptr;
             for (int k = 0; k < 4; ++k) pushed_[k] = o.pushed_[k];
@@ -125,7 +127,61 @@ public:
     {
         materialize();
         push_rates();
+        push_input_rates();
         check(nc_run(net_, steps));
+    }
+
+    // NeuCor::setInputRateArray (src/NeuCor.cpp:46-64).  The array stays borrowed: its
+    // rates are read again before every run, as the reference does.
+    void setInputRateArray(float inputs[], unsigned inputCount, coord3 inputPositions[] = nullptr,
+                           float inputRadius[] = nullptr)
+    {
+        materialize();
+        std::vector<float> xyz;
+        if (inputPositions)
+            for (unsigned i = 0; i < inputCount; ++i) {
+                xyz.push_back(inputPositions[i].x);
+                xyz.push_back(inputPositions[i].y);
+                xyz.push_back(inputPositions[i].z);
+            }
+        check(nc_set_input_rate_array(net_, inputs, inputCount, inputPositions ? xyz.data() : nullptr, inputRadius));
+        inputArray_ = inputs;
+        inputRates_.assign(inputs, inputs + inputCount);
+    }
+    void addInputOffset(unsigned inputID, float t)        // src/NeuCor.cpp:66-68
+    {
+        materialize();
+        check(nc_add_input_offset(net_, (int32_t)inputID, t));
+    }
+    void setDetectors(unsigned detectorNumber, coord3 detectorPositions[] = nullptr,
+                      float detectorRadius[] = nullptr)  // src/NeuCor.cpp:70-77
+    {
+        materialize();
+        std::vector<float> xyz;
+        if (detectorPositions)
+            for (unsigned i = 0; i < detectorNumber; ++i) {
+                xyz.push_back(detectorPositions[i].x);
+                xyz.push_back(detectorPositions[i].y);
+                xyz.push_back(detectorPositions[i].z);
+            }
+        check(nc_set_detectors(net_, (int32_t)detectorNumber, detectorPositions ? xyz.data() : nullptr,
+                               detectorRadius));
+    }
+    float getDetectorVoltage(unsigned ID)                  // src/NeuCor.cpp:75-77
+    {
+        materialize();
+        float v = 0.0f;
+        check(nc_get_detector_voltage(net_, (int32_t)ID, &v));
+        return v;
+    }
+    std::vector<float> getDetectorVoltages()               // src/NeuCor.cpp:79-83
+    {
+        materialize();
+        int32_t n = 0;
+        check(nc_get_detector_voltages(net_, nullptr, 0, &n));
+        std::vector<float> v((size_t)n);
+        if (n) check(nc_get_detector_voltages(net_, v.data(), n, &n));
+        return v;
     }
     float getTime() const
     {
@@ -258,7 +314,19 @@ private:
     std::vector<float> xyz_;
     std::vector<int32_t> from_, to_;
     std::vector<float> w_;
+    void push_input_rates()
+    {
+        if (!inputArray_) return;
+        bool changed = false;
+        for (size_t i = 0; i < inputRates_.size(); ++i) changed |= inputRates_[i] != inputArray_[i];
+        if (!changed) return;
+        inputRates_.assign(inputArray_, inputArray_ + inputRates_.size());
+        check(nc_set_input_rates(net_, (int32_t)inputRates_.size(), inputRates_.data()));
+    }
+
     std::vector<nc_group> groups_;
+    const float* inputArray_ = nullptr;  // borrowed, as NeuCor::inputArray
+    std::vector<float> inputRates_;      // the rates last pushed
     nc_net* net_ = nullptr;
     float pushed_[4] = {0, 0, 0, 0};
 };

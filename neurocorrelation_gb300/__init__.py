@@ -128,6 +128,9 @@ def load_library() -> ctypes.CDLL:
         "nc_server_poll": ([P, P, I32, P], I32), "nc_server_drain": ([P], I32),
         "nc_server_fetch": ([P, I64, P, P], I32), "nc_server_get_stats": ([P, P], I32),
         "nc_server_destroy": ([P], I32), "nc_run_noalloc": ([P, I32, P], I32),
+        "nc_set_input_rates": ([P, I32, P], I32), "nc_add_input_offset": ([P, I32, F], I32),
+        "nc_set_detectors": ([P, I32, P, P], I32), "nc_get_detector_voltages": ([P, P, I32, P], I32),
+        "nc_get_detector_voltage": ([P, I32, P], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -323,10 +326,53 @@ class NeuCor:
         _check(self._lib.nc_set_input_groups(self._h, len(self._groups), ctypes.cast(arr, ctypes.c_void_p)))
 
     def setInputRateArray(self, inputs, inputCount=None, inputPositions=None, inputRadius=None):
-        """NeuCor::setInputRateArray (src/NeuCor.cpp:46-64): periodic firers are not in the
-        stepped GPU model yet; raises NeuCorError(unsupported)."""
-        rates = np.ascontiguousarray(inputs, dtype=np.float32)
-        _check(self._lib.nc_set_input_rate_array(self._handle(), _p(rates), rates.size, None, None))
+        """NeuCor::setInputRateArray (src/NeuCor.cpp:46-64): periodic input firers at the
+        given rates (Hz); positions (n x 3) and radii for the firers appended by this call
+        (None: random positions from the C library's rand() and radius 1)."""
+        rates = np.ascontiguousarray(inputs, dtype=np.float32).ravel()
+        n = rates.size if inputCount is None else int(inputCount)
+        xyz = rad = None
+        if inputPositions is not None:
+            xyz = np.ascontiguousarray(inputPositions, dtype=np.float32).reshape(-1, 3)
+            rad = np.ascontiguousarray(inputRadius if inputRadius is not None else np.ones(len(xyz)),
+                                       dtype=np.float32)
+        _check(self._lib.nc_set_input_rate_array(self._handle(), _p(rates), n,
+                                                 _p(xyz) if xyz is not None else None,
+                                                 _p(rad) if rad is not None else None))
+
+    def set_input_rates(self, rates):
+        """New frequencies of the first len(rates) firers (the reference's borrowed array)."""
+        r = np.ascontiguousarray(rates, dtype=np.float32).ravel()
+        _check(self._lib.nc_set_input_rates(self._handle(), r.size, _p(r)))
+
+    def addInputOffset(self, inputID, t):
+        """NeuCor::addInputOffset (src/NeuCor.cpp:66-68)."""
+        _check(self._lib.nc_add_input_offset(self._handle(), int(inputID), float(t)))
+
+    def setDetectors(self, detectorNumber, detectorPositions=None, detectorRadius=None):
+        """NeuCor::setDetectors (src/NeuCor.cpp:70-77)."""
+        xyz = rad = None
+        if detectorPositions is not None:
+            xyz = np.ascontiguousarray(detectorPositions, dtype=np.float32).reshape(-1, 3)
+            rad = np.ascontiguousarray(detectorRadius if detectorRadius is not None else np.ones(len(xyz)),
+                                       dtype=np.float32)
+        _check(self._lib.nc_set_detectors(self._handle(), int(detectorNumber), _p(xyz) if xyz is not None else None,
+                                          _p(rad) if rad is not None else None))
+
+    def getDetectorVoltages(self):
+        """NeuCor::getDetectorVoltages (src/NeuCor.cpp:79-83)."""
+        cnt = ctypes.c_int32()
+        _check(self._lib.nc_get_detector_voltages(self._handle(), None, 0, ctypes.byref(cnt)))
+        out = np.zeros(cnt.value, dtype=np.float32)
+        if cnt.value:
+            _check(self._lib.nc_get_detector_voltages(self._handle(), _p(out), cnt.value, ctypes.byref(cnt)))
+        return out
+
+    def getDetectorVoltage(self, ID):
+        """NeuCor::getDetectorVoltage (src/NeuCor.cpp:75-77)."""
+        v = ctypes.c_float()
+        _check(self._lib.nc_get_detector_voltage(self._handle(), int(ID), ctypes.byref(v)))
+        return float(v.value)
 
     def schedule_fire(self, ids):
         """Neuron::scheduleFire for the next step (src/NeuCor.cpp:658-661)."""

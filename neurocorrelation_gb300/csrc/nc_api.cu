@@ -153,13 +153,159 @@ int nc_set_input_groups(nc_net* net, int32_t n_groups, const nc_group* groups)
     return NC_OK;
 }
 
+// randomUnit(), src/NeuCor.cpp:12-14 (the C library's rand(), as the reference)
+static float random_unit() { return (float)rand() / (float)RAND_MAX; }
+
+// Neurons closer than `radius` to `a` (InputFirer / VoltageDetector constructors,
+// src/NeuCor.cpp:323-327, 353-357), as caller ids in ascending order.
+static std::vector<int32_t> near_ids(const nc::NetHost& h, const float a[3], float radius)
+{
+    std::vector<int32_t> out;
+    for (int32_t j = 0; j < h.n; ++j)
+        if (nc::get_dist(&h.xyz[3 * (size_t)j], a) < radius) out.push_back(j);
+    return out;
+}
+
+// Uploads the firer set: state (lastFire) of the first `keep` firers carried over.
+static int upload_firers(nc_net* net, const std::vector<NcFirer>& old, const std::vector<float>& rates)
+{
+    std::vector<NcFirer> f(net->firer_near.size());
+    std::vector<int32_t> near;
+    for (size_t i = 0; i < f.size(); ++i) {
+        f[i].net = 0;
+        f[i].last = i < old.size() ? old[i].last : 0.0f;  // InputFirer: lastFire(0.0)
+        f[i].rate = i < rates.size() ? rates[i] : 0.0f;
+        f[i].near_begin = (int32_t)near.size();
+        for (int32_t id : net->firer_near[i]) near.push_back(net->host.slot_of[(size_t)id]);
+        f[i].near_end = (int32_t)near.size();
+    }
+    NC_CALL(net->eng, set_firers, f, near);
+    return NC_OK;
+}
+
 int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
                             const float* radius)
 {
-    (void)rates_hz; (void)count; (void)xyz; (void)radius;
-    if (!net) return fail(NC_ERR_INVALID, "null handle");
-    return fail(NC_ERR_UNSUPPORTED, "periodic input firers are not implemented in the stepped GPU model; "
-                                    "use nc_set_input_groups or nc_schedule_fire");
+    NC_NEED(net);
+    if (xyz && !radius) return fail(NC_ERR_INVALID, "positions given without radii");
+    if (count > (1u << 24)) return fail(NC_ERR_INVALID, "too many input firers");
+    std::vector<NcFirer> old;
+    NC_CALL(net->eng, read_firers, old);
+    const size_t cur = net->firer_near.size();
+    // NeuCor::setInputRateArray (src/NeuCor.cpp:46-64): firers are appended (the i-th new
+    // one taking position and radius i) or removed from the end to match the count
+    if (count > cur) {
+        for (size_t i = 0; i < count - cur; ++i) {
+            float a[3];
+            float r = 1.0f;
+            if (xyz) {
+                a[0] = xyz[3 * i];
+                a[1] = xyz[3 * i + 1];
+                a[2] = xyz[3 * i + 2];
+                r = radius[i];
+            } else {  // InputFirer's random position (src/NeuCor.cpp:312-313)
+                for (int d = 0; d < 3; ++d) a[d] = (random_unit() - 0.5f) * 5.f;
+            }
+            net->firer_xyz.insert(net->firer_xyz.end(), a, a + 3);
+            net->firer_radius.push_back(r);
+            net->firer_near.push_back(near_ids(net->host, a, r));
+        }
+    } else {
+        net->firer_near.resize(count);
+        net->firer_xyz.resize(3 * (size_t)count);
+        net->firer_radius.resize(count);
+    }
+    std::vector<float> rates(count, 0.0f);
+    if (rates_hz) std::copy(rates_hz, rates_hz + count, rates.begin());
+    return upload_firers(net, old, rates);
+}
+
+int nc_set_input_rates(nc_net* net, int32_t count, const float* rates_hz)
+{
+    NC_NEED(net);
+    if (count < 0 || (count > 0 && !rates_hz) || (size_t)count > net->firer_near.size())
+        return fail(NC_ERR_INVALID, "more rates than input firers");
+    std::vector<NcFirer> f;
+    NC_CALL(net->eng, read_firers, f);
+    for (int32_t i = 0; i < count; ++i) f[(size_t)i].rate = rates_hz[i];
+    NC_CALL(net->eng, write_firers, f);
+    return NC_OK;
+}
+
+int nc_add_input_offset(nc_net* net, int32_t id, float t_ms)
+{
+    NC_NEED(net);
+    if (id < 0 || (size_t)id >= net->firer_near.size()) return fail(NC_ERR_INVALID, "no such input firer");
+    std::vector<NcFirer> f;
+    NC_CALL(net->eng, read_firers, f);
+    f[(size_t)id].last += t_ms;  // NeuCor::addInputOffset (src/NeuCor.cpp:66-68)
+    NC_CALL(net->eng, write_firers, f);
+    return NC_OK;
+}
+
+int nc_set_detectors(nc_net* net, int32_t count, const float* xyz, const float* radius)
+{
+    NC_NEED(net);
+    if (count < 0 || count > (1 << 24)) return fail(NC_ERR_INVALID, "bad detector count");
+    if (xyz && !radius) return fail(NC_ERR_INVALID, "positions given without radii");
+    // NeuCor::setDetectors (src/NeuCor.cpp:70-77) appends `count` detectors
+    for (int32_t i = 0; i < count; ++i) {
+        float a[3];
+        float r = 1.0f;
+        if (xyz) {
+            a[0] = xyz[3 * (size_t)i];
+            a[1] = xyz[3 * (size_t)i + 1];
+            a[2] = xyz[3 * (size_t)i + 2];
+            r = radius[i];
+        } else {  // VoltageDetector's random position (src/NeuCor.cpp:349-350)
+            for (int d = 0; d < 3; ++d) a[d] = (random_unit() - 0.5f) * 3.f;
+        }
+        const std::vector<int32_t> ids = near_ids(net->host, a, r);
+        net->det_near.insert(net->det_near.end(), ids.begin(), ids.end());
+        net->det_ptr.push_back((int32_t)net->det_near.size());
+    }
+    // device copies: near ids, then the pointer array; one voltage per detector
+    if (net->d_det) cudaFree(net->d_det);
+    if (net->d_volt) cudaFree(net->d_volt);
+    net->d_det = nullptr;
+    net->d_volt = nullptr;
+    std::vector<int32_t> flat(net->det_near);
+    flat.insert(flat.end(), net->det_ptr.begin(), net->det_ptr.end());
+    const size_t n_det = net->det_ptr.size() - 1;
+    cudaError_t e = cudaMalloc(&net->d_det, sizeof(int32_t) * flat.size());
+    if (e == cudaSuccess) e = cudaMalloc(&net->d_volt, sizeof(float) * std::max<size_t>(n_det, 1));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(net->d_det, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("detector tables", e));
+    return NC_OK;
+}
+
+int nc_get_detector_voltages(nc_net* net, float* out, int32_t capacity, int32_t* count)
+{
+    NC_NEED(net);
+    const int32_t n_det = (int32_t)net->det_ptr.size() - 1;
+    if (count) *count = n_det;
+    if (!out || n_det == 0) return NC_OK;
+    if (capacity < n_det) return fail(NC_ERR_INVALID, "voltage buffer too small");
+    const auto& sl = net->eng.slots[0];
+    const int32_t* near = net->d_det;
+    const int32_t* ptr = net->d_det + net->det_near.size();
+    if (nc::launch_detector_voltages(net->eng.P, sl.neuron_base, near, ptr, n_det, net->d_volt, net->eng.stream))
+        return fail(NC_ERR_CUDA, nc::cuda_msg("detector voltages", cudaGetLastError()));
+    NC_CALL(net->eng, download, out, (const float*)net->d_volt, (size_t)n_det);
+    return NC_OK;
+}
+
+int nc_get_detector_voltage(nc_net* net, int32_t id, float* out)
+{
+    NC_NEED(net);
+    const int32_t n_det = (int32_t)net->det_ptr.size() - 1;
+    if (!out || id < 0 || id >= n_det) return fail(NC_ERR_INVALID, "no such detector");  // .at(ID) throws
+    std::vector<float> v((size_t)n_det);
+    const int rc = nc_get_detector_voltages(net, v.data(), n_det, nullptr);
+    if (rc != NC_OK) return rc;
+    *out = v[(size_t)id];
+    return NC_OK;
 }
 
 int nc_set_rates(nc_net* net, float learning_rate, float presynaptic_factor, float postsynaptic_factor)

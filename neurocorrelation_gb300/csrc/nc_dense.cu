@@ -534,6 +534,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
             const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
             float pot = P.pot[pj];
             const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
+            const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
             bool forced = (fw >> lane) & 1u;
             if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
             // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
@@ -587,7 +588,8 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
             pot = (pot - -70.0f) * D.leak + -70.0f;
             // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
             const bool can = (lf == NC_NEVER) || (t - lf >= kc);
-            fired = (-55.0f < pot || forced) && can;
+            // an input firer's Neuron::fire has no threshold or refractory test
+            fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
             if (fired) {
                 lf = t;
                 P.lf[pj] = t;
@@ -601,6 +603,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
         if (lane == 0) {
             P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
             P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
+            P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
             if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
                 D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
         }

@@ -36,6 +36,7 @@
 
 // Device error codes (NcPools::dev_err).
 #define NC_DEV_ERR_STAGE_TIMEOUT 1u  // a bulk copy into shared memory did not complete in time
+#define NC_DEV_ERR_FIRER_LOOP 2u     // an input firer's schedule did not advance (capped)
 
 // Draw streams (third Philox counter word).
 #define NC_STREAM_BACKGROUND 1u
@@ -93,7 +94,15 @@ struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8
     int32_t first;       // local id of the first neuron (multiple of 32), or first chunk
 };
 
-constexpr int NC_SPAN_CHUNKS = 8;  // 32-synapse chunks per span of the dense synapse pass
+constexpr int NC_SPAN_CHUNKS = 8;
+
+struct NcFirer {         // periodic input firer (InputFirer, src/NeuCor.cpp:305-345)
+    int32_t net;
+    float last;          // InputFirer::lastFire, ms
+    float rate;          // its entry of the rate array, Hz
+    int32_t near_begin;  // neuron slots firer_near[near_begin .. near_end)
+    int32_t near_end;
+};  // 32-synapse chunks per span of the dense synapse pass
 
 struct NcPools {
     // neurons
@@ -131,6 +140,10 @@ struct NcPools {
     uint32_t* ring;
     uint32_t* fired;     // 2 parities x total_words
     uint32_t* forced;    // 2 parities x total_words
+    uint32_t* ufire;     // 2 parities x total_words: input-firer fires (no threshold, no refractory)
+    NcFirer* firers;
+    int32_t n_firers;
+    int32_t* firer_near;
     int64_t total_words;
     // fired list (global, 2 parities)
     int2* fired_list;    // (net, local id)
@@ -215,6 +228,12 @@ int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);
+// Input firers (nc_inputs.cu): each firer's schedule for the interval after the last
+// completed step of its net; fires land in that net's ufire bits of the next step.
+int launch_input_firers(const NcPools& P, void* stream);
+// Mean potential of each detector's near neurons (caller ids; near_ptr has count+1 entries).
+int launch_detector_voltages(const NcPools& P, int32_t neuron_base, const int32_t* near, const int32_t* near_ptr,
+                             int32_t count, float* out, void* stream);
 int launch_raster_to_ids(const uint32_t* in, uint32_t* out, const int32_t* slot_of, int32_t n, int32_t n_words,
                          int32_t rows, void* stream);
 }  // namespace nc

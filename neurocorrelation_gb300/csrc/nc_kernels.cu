@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
             int64_t s0 = 0, s1 = 0;
             int32_t r0 = 0, r1 = 0;
             float pot = 0.0f;
-            uint32_t fw = 0;
+            uint32_t fw = 0, uw = 0;
             if (live) {
                 lf = P.lf[pj];
                 s0 = P.in_ptr[pb];
@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                 r1 = P.ring_off[pb + 1];
                 pot = P.pot[pj];
                 fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
+                uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
             }
             const int32_t prev = t - 1;
             const bool stdp = prev >= 1 && D.stdp_done < prev;
@@ -237,7 +238,8 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                 pot = (pot - -70.0f) * D.leak + -70.0f;
                 // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
                 const bool can = (lf == NC_NEVER) || (t - lf >= D.kc);
-                fired = (-55.0f < pot || forced) && can;
+                // an input firer's Neuron::fire has no threshold or refractory test
+                fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
                 if (fired) {
                     lf = t;
                     P.lf[pj] = t;
@@ -251,6 +253,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
             if (lane == 0) {
                 P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
                 P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
+                P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
                 if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
                     D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
             }

@@ -26,6 +26,8 @@ Engine::~Engine()
 {
     release_graph();
     if (stream) cudaStreamSynchronize(stream);
+    if (firers_buf_) cudaFree(firers_buf_);
+    if (near_buf_) cudaFree(near_buf_);
     for (void* p : allocs_) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -201,6 +203,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     P.total_words = std::max<int64_t>(words, 1);
     NC_ALLOC(P.fired, uint32_t, 2 * P.total_words);
     NC_ALLOC(P.forced, uint32_t, 2 * P.total_words);
+    NC_ALLOC(P.ufire, uint32_t, 2 * P.total_words);
     P.fired_cap = dense ? 0 : std::max<int64_t>(neurons, 1);
     if (!dense) NC_ALLOC(P.fired_list, int2, 2 * P.fired_cap);
     NC_ALLOC(P.fired_count, int32_t, 2);
@@ -327,8 +330,62 @@ int Engine::step(int64_t ticks, std::string& err)
 
 int Engine::launch_tick(cudaStream_t s)
 {
-    if (dense) return launch_step_dense(P, L, s);
-    return launch_neuron_step(P, L, s) | launch_spike_launch(P, L, s);
+    int rc = dense ? launch_step_dense(P, L, s) : (launch_neuron_step(P, L, s) | launch_spike_launch(P, L, s));
+    if (P.n_firers > 0) rc |= launch_input_firers(P, s);
+    return rc;
+}
+
+int Engine::set_firers(const std::vector<NcFirer>& firers, const std::vector<int32_t>& near, std::string& err)
+{
+    release_graph();  // the captured ticks change
+    NC_CK(cudaStreamSynchronize(stream));
+    if (firers_buf_) cudaFree(firers_buf_);
+    if (near_buf_) cudaFree(near_buf_);
+    firers_buf_ = nullptr;
+    near_buf_ = nullptr;
+    P.firers = nullptr;
+    P.firer_near = nullptr;
+    P.n_firers = 0;
+    if (firers.empty()) return NC_OK;
+    NC_CK(cudaMalloc(&firers_buf_, sizeof(NcFirer) * firers.size()));
+    NC_CK(cudaMalloc(&near_buf_, sizeof(int32_t) * std::max<size_t>(near.size(), 1)));
+    NC_CK(cudaMemcpyAsync(firers_buf_, firers.data(), sizeof(NcFirer) * firers.size(), cudaMemcpyHostToDevice, stream));
+    if (!near.empty())
+        NC_CK(cudaMemcpyAsync(near_buf_, near.data(), sizeof(int32_t) * near.size(), cudaMemcpyHostToDevice, stream));
+    P.firers = (NcFirer*)firers_buf_;
+    P.firer_near = (int32_t*)near_buf_;
+    P.n_firers = (int32_t)firers.size();
+    return evaluate_firers(err);
+}
+
+int Engine::evaluate_firers(std::string& err)
+{
+    if (launch_input_firers(P, stream)) {
+        err = cuda_msg("input firers", cudaGetLastError());
+        return NC_ERR_CUDA;
+    }
+    NC_CK(cudaStreamSynchronize(stream));
+    return NC_OK;
+}
+
+int Engine::read_firers(std::vector<NcFirer>& out, std::string& err)
+{
+    out.resize((size_t)P.n_firers);
+    if (P.n_firers == 0) return NC_OK;
+    NC_CK(cudaMemcpyAsync(out.data(), P.firers, sizeof(NcFirer) * out.size(), cudaMemcpyDeviceToHost, stream));
+    NC_CK(cudaStreamSynchronize(stream));
+    return NC_OK;
+}
+
+int Engine::write_firers(const std::vector<NcFirer>& in, std::string& err)
+{
+    if ((int32_t)in.size() != P.n_firers) {
+        err = "firer count mismatch";
+        return NC_ERR_INVALID;
+    }
+    if (P.n_firers == 0) return NC_OK;
+    NC_CK(cudaMemcpyAsync(P.firers, in.data(), sizeof(NcFirer) * in.size(), cudaMemcpyHostToDevice, stream));
+    return evaluate_firers(err);
 }
 
 int Engine::step_timed(int64_t ticks, float* ms, std::string& err)
@@ -364,6 +421,10 @@ int Engine::time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::str
             return NC_ERR_CUDA;
         }
         NC_CK(cudaEventRecord(ev[3 * k + 2], stream));
+        if (P.n_firers > 0 && launch_input_firers(P, stream)) {
+            err = "launch";
+            return NC_ERR_CUDA;
+        }
     }
     NC_CK(cudaStreamSynchronize(stream));
     double sa = 0, sb = 0;

@@ -60,8 +60,14 @@ public:
     int device = 0;
     int graph_ticks = 32;
     bool dense = true;  // NC_STEP_DENSE: one launch per step (nc_dense.cu)
-    // Launches one tick of the engine's form on `s` (no graph).
+    // Launches one tick of the engine's form on `s` (no graph), the input firers' schedule
+    // included.
     int launch_tick(cudaStream_t s);
+    // Periodic input firers (replaces the set), their state read and written back; every
+    // change evaluates the interval after the last completed step at once.
+    int set_firers(const std::vector<NcFirer>& firers, const std::vector<int32_t>& near, std::string& err);
+    int read_firers(std::vector<NcFirer>& out, std::string& err);
+    int write_firers(const std::vector<NcFirer>& in, std::string& err);
 
 private:
     int capture_graph(std::string& err);
@@ -70,6 +76,9 @@ private:
     T* alloc(size_t count, std::string& err);
     std::vector<void*> allocs_;
     cudaGraphExec_t graph_ = nullptr;
+    int evaluate_firers(std::string& err);
+    void* firers_buf_ = nullptr;
+    void* near_buf_ = nullptr;
     int32_t* d_ids_ = nullptr;
     int ids_cap_ = 0;
     unsigned long long* d_stats_ = nullptr;

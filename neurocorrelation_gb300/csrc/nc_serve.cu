@@ -253,6 +253,7 @@ int nc_server::init(std::string& err)
     P.total_words = word_cap;
     S_AL(P.fired, uint32_t, 2 * word_cap);
     S_AL(P.forced, uint32_t, 2 * word_cap);
+    S_AL(P.ufire, uint32_t, 2 * word_cap);
     P.fired_cap = dense ? 0 : neuron_cap;
     if (!dense) S_AL(P.fired_list, int2, 2 * neuron_cap);
     S_AL(P.fired_count, int32_t, 2);
@@ -452,6 +453,7 @@ int nc_server::admit(Resident& r, std::string& err)
     for (int par = 0; par < 2; ++par) {
         S_CK(cudaMemsetAsync(P.fired + par * P.total_words + wb, 0, sizeof(uint32_t) * r.words, stream));
         S_CK(cudaMemsetAsync(P.forced + par * P.total_words + wb, 0, sizeof(uint32_t) * r.words, stream));
+        S_CK(cudaMemsetAsync(P.ufire + par * P.total_words + wb, 0, sizeof(uint32_t) * r.words, stream));
     }
     S_CK(put(P.tables, h.tables, tb, stream));
     if (!h.groups.empty()) S_CK(put(P.groups, h.groups, (int64_t)r.slot * kGroupsPerNet, stream));

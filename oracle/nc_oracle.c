@@ -106,6 +106,15 @@ struct ncs_net {
     int32_t* act_start;   /* activityStartTime as a step */
     int32_t* busy;        /* in-synapses not FREE, to skip idle neurons */
     uint8_t* forced;      /* requests for step cur+1 (scheduledFireTime == T) */
+    uint8_t* ufire;       /* InputFirer fires for step cur+1 (Neuron::fire, no threshold) */
+    float* xyz;           /* neuron positions (NeuCor::positions) */
+
+    /* periodic input firers (InputFirer, NeuCor.cpp:305-345) */
+    int32_t n_firers;
+    float* f_last;        /* InputFirer::lastFire, ms */
+    float* f_rate;        /* the firer's entry of the rate array, Hz */
+    int64_t* f_ptr;       /* near lists: f_ids[f_ptr[i] .. f_ptr[i+1]) */
+    int32_t* f_ids;
 
     /* arrivals bucketed by step modulo ring */
     int32_t ring;
@@ -205,6 +214,8 @@ ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* s
     h->n = n;
     h->n_input = n_syn;
     h->p = *params;
+    h->xyz = (float*)xcalloc((size_t)n * 3, sizeof(float));  /* positions, for the firers' near lists */
+    if (xyz) memcpy(h->xyz, xyz, sizeof(float) * 3 * (size_t)n);
     h->dt = params->run_speed;
     h->kc = 1;
     while (!(2.0f < kdt(h, h->kc))) h->kc++;
@@ -297,6 +308,7 @@ ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* s
     h->act_start = (int32_t*)xcalloc((size_t)n, sizeof(int32_t));
     h->busy = (int32_t*)xcalloc((size_t)n, sizeof(int32_t));
     h->forced = (uint8_t*)xcalloc((size_t)n, 1);
+    h->ufire = (uint8_t*)xcalloc((size_t)n, 1);
     for (int32_t j = 0; j < n; ++j) {
         h->pot[j] = -70.0f;   /* setPotential(baselevel) */
         h->activity[j] = 0.0f;
@@ -326,7 +338,8 @@ void ncs_destroy(ncs_net* h)
     free(h->out_syn); free(h->input_to_csc); free(h->w); free(h->inh); free(h->depol);
     free(h->arr); free(h->t_arr); free(h->launch_step); free(h->stdp_step);
     free(h->pot); free(h->activity); free(h->lf); free(h->firings); free(h->act_start);
-    free(h->busy); free(h->forced);
+    free(h->busy); free(h->forced); free(h->ufire);
+    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids); free(h->xyz);
     if (h->bucket)
         for (int32_t r = 0; r < h->ring; ++r) free(h->bucket[r]);
     free(h->bucket); free(h->bucket_len); free(h->bucket_cap);
@@ -535,8 +548,10 @@ static float ap_value(float x)
     return (float)v;
 }
 
-/* Neuron::run at step t >= 1, NeuCor.cpp:619-641. */
-static void neuron_run(ncs_net* h, int32_t j, int32_t t, int forced)
+/* Neuron::run at step t >= 1, NeuCor.cpp:619-641.  `input`: an InputFirer fired the
+ * neuron in the interval before t (InputFirer::run -> Neuron::fire, NeuCor.cpp:
+ * 326-331), which the stepped model places at t: no threshold or refractory test. */
+static void neuron_run(ncs_net* h, int32_t j, int32_t t, int forced, int input)
 {
     const float deltaT = h->dt;
     const float currentT = kdt(h, t);
@@ -558,13 +573,86 @@ static void neuron_run(ncs_net* h, int32_t j, int32_t t, int forced)
     /* charge_passive, NeuCor.cpp:677-680 */
     h->pot[j] = ((float)h->pot[j] - -70.0f) * powf(0.5f, deltaT) + -70.0f;
     /* charge_thresholdCheck, NeuCor.cpp:682-686 (vesicles never drop below 0) */
-    if ((-55.0f < h->pot[j] || forced) &&
-        (h->lf[j] == NEVER || 2.0f < kdt(h, t - h->lf[j])))
+    if (input || ((-55.0f < h->pot[j] || forced) &&
+                  (h->lf[j] == NEVER || 2.0f < kdt(h, t - h->lf[j]))))
         fire(h, j, t);
     /* AP, NeuCor.cpp:706-714 */
     if (!(h->lf[j] == NEVER || 2.0f < kdt(h, t - h->lf[j]))) h->pot[j] = ap_value(kdt(h, t - h->lf[j]));
     /* setActivity, NeuCor.cpp:640 */
     h->activity[j] = (float)(h->firings[j] / (((float)currentT - kdt(h, h->act_start[j])) / 10.0));
+}
+
+/* InputFirer::schedule(deltaT, frequency), NeuCor.cpp:333-345, at currentT = t*dt:
+ * the fire times lastFire + k*1000/frequency that fall in (currentT, currentT+deltaT),
+ * in the reference's float/double arithmetic.  Returns 1 if any falls there.  The loop
+ * is capped (NCS_FIRER_LOOP_CAP passes); the reference loops without end when the
+ * period does not advance fireTime. */
+#define NCS_FIRER_LOOP_CAP (1 << 20)
+static int firer_schedule(float* last, float dt, float frequency, float currentT)
+{
+    int fired = 0;
+    if (frequency == 0.0f) return 0;
+    if (*last != *last) *last = 0.0f;
+    int32_t pass = 0;
+    for (float fireTime = (float)((double)*last + 1000.0 / frequency);
+         fireTime < currentT + dt && pass < NCS_FIRER_LOOP_CAP;
+         fireTime = (float)((double)fireTime + 1000.0 / frequency), ++pass) {
+        if (currentT < fireTime) {
+            fired = 1;
+            *last = fireTime;
+        }
+    }
+    return fired;
+}
+
+static void firers_schedule(ncs_net* h, int32_t t)
+{
+    const float currentT = kdt(h, t);
+    for (int32_t i = 0; i < h->n_firers; ++i)
+        if (firer_schedule(&h->f_last[i], h->dt, h->f_rate[i], currentT))
+            for (int64_t k = h->f_ptr[i]; k < h->f_ptr[i + 1]; ++k) h->ufire[h->f_ids[k]] = 1;
+}
+
+int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* xyz, const float* radius)
+{
+    if (!h || count < 0 || (count > 0 && (!xyz || !radius))) return -1;
+    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids);
+    h->n_firers = count;
+    h->f_last = (float*)xcalloc((size_t)count, sizeof(float));  /* lastFire(0.0), NeuCor.cpp:311 */
+    h->f_rate = (float*)xcalloc((size_t)count, sizeof(float));
+    h->f_ptr = (int64_t*)xcalloc((size_t)count + 1, sizeof(int64_t));
+    int64_t total = 0;
+    for (int32_t i = 0; i < count; ++i)
+        for (int32_t j = 0; j < h->n; ++j)
+            if (get_dist(&h->xyz[3 * (int64_t)j], &xyz[3 * (int64_t)i]) < radius[i]) ++total;
+    h->f_ids = (int32_t*)xcalloc((size_t)total, sizeof(int32_t));
+    total = 0;
+    /* near: every neuron closer than radius, in id order (NeuCor.cpp:323-327) */
+    for (int32_t i = 0; i < count; ++i) {
+        h->f_rate[i] = rates ? rates[i] : 0.0f;
+        for (int32_t j = 0; j < h->n; ++j)
+            if (get_dist(&h->xyz[3 * (int64_t)j], &xyz[3 * (int64_t)i]) < radius[i]) h->f_ids[total++] = j;
+        h->f_ptr[i + 1] = total;
+    }
+    firers_schedule(h, h->cur);
+    return 0;
+}
+
+int ncs_set_firer_rates(ncs_net* h, int32_t count, const float* rates)
+{
+    if (!h || count < 0 || count > h->n_firers) return -1;
+    for (int32_t i = 0; i < count; ++i) h->f_rate[i] = rates[i];
+    firers_schedule(h, h->cur);
+    return 0;
+}
+
+/* NeuCor::addInputOffset, NeuCor.cpp:66-68 */
+int ncs_add_firer_offset(ncs_net* h, int32_t id, float t)
+{
+    if (!h || id < 0 || id >= h->n_firers) return -1;
+    h->f_last[id] += t;
+    firers_schedule(h, h->cur);
+    return 0;
 }
 
 int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
@@ -575,8 +663,9 @@ int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
         int32_t t = h->cur + 1;
         for (int32_t j = 0; j < h->n; ++j) {
             int forced = h->forced[j] || input_request(h, j, t);
-            neuron_run(h, j, t, forced);
+            neuron_run(h, j, t, forced, h->ufire[j]);
         }
+        memset(h->ufire, 0, (size_t)h->n);
         /* spikes arriving at T: Synapse::run, NeuCor.cpp:718-726 */
         int32_t slot = t & (h->ring - 1);
         for (int64_t q = 0; q < h->bucket_len[slot]; ++q) {
@@ -589,6 +678,8 @@ int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
         /* background fires for step t+1, NeuCor.cpp:604-607 */
         memset(h->forced, 0, (size_t)h->n);
         if (h->p.background_firing && h->n > 0) draw_background(h, t);
+        /* input firers schedule the interval after t (NeuCor.cpp:599-602) */
+        firers_schedule(h, t);
         if (raster) {
             uint8_t* rr = raster + (int64_t)r * row;
             memset(rr, 0, (size_t)row);

@@ -88,6 +88,9 @@ def lib() -> ctypes.CDLL:
         L.ncs_set_groups.argtypes = [P, ctypes.c_int32, P]
         L.ncs_set_rates.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.ncs_schedule_fire.argtypes = [P, ctypes.c_int32, P]
+        L.ncs_set_firers.argtypes = [P, ctypes.c_int32, P, P, P]
+        L.ncs_set_firer_rates.argtypes = [P, ctypes.c_int32, P]
+        L.ncs_add_firer_offset.argtypes = [P, ctypes.c_int32, ctypes.c_float]
         L.ncs_run.argtypes = [P, ctypes.c_int32, P, P]
         L.ncs_step.restype = ctypes.c_int32
         L.ncs_step.argtypes = [P]
@@ -171,6 +174,21 @@ class OracleS:
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         if lib().ncs_schedule_fire(self.h, int(ids.size), _ptr(ids)) != 0:
             raise ValueError("bad neuron id")
+
+    def set_firers(self, rates, xyz, radius):
+        """Periodic input firers (NeuCor::setInputRateArray + InputFirer)."""
+        r = np.ascontiguousarray(rates, dtype=np.float32)
+        x = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        rad = np.ascontiguousarray(radius, dtype=np.float32)
+        assert lib().ncs_set_firers(self.h, len(r), _ptr(r), _ptr(x), _ptr(rad)) == 0
+
+    def set_firer_rates(self, rates):
+        r = np.ascontiguousarray(rates, dtype=np.float32)
+        assert lib().ncs_set_firer_rates(self.h, len(r), _ptr(r)) == 0
+
+    def add_firer_offset(self, firer: int, t_ms: float):
+        """NeuCor::addInputOffset."""
+        assert lib().ncs_add_firer_offset(self.h, int(firer), float(t_ms)) == 0
 
     def set_rates(self, learning_rate, pre_factor, post_factor):
         lib().ncs_set_rates(self.h, learning_rate, pre_factor, post_factor)
