@@ -240,6 +240,15 @@ int nc_delete_neuron(nc_net* net, int32_t id);
  * from/to/weight (n*k).  Lengths follow coord3::getDist (src/NeuCor.h:16-18). */
 int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, float* xyz, int32_t* syn_from,
                  int32_t* syn_to, float* syn_weight);
+/* The network nc_build_knn describes, passed to nc_create — built on the GPU instead:
+ * positions, the grid-hash neighbour search, weights and the in-synapse rows are
+ * computed on the device (identical bits: same draws, same distances, same (distance,
+ * id) order, same rows).  Dense form only (params->step_mode = NC_STEP_DENSE; an event-
+ * form request, or one past the device builder's capacities — k > 512, more than 16,384
+ * neighbour candidates or 2,048 in-synapses per neuron — is built on the host).
+ * xyz_out (3n floats, may be NULL) receives the positions. */
+int nc_create_knn(int32_t n, int32_t k, float density, uint64_t seed, const nc_params* params, float* xyz_out,
+                  nc_net** out);
 /* The reference constructor NeuCor(n) (src/NeuCor.cpp:17-42) in three calls that draw
  * from the C library's rand() in the reference's order, so after srand(s) they build
  * the network the reference builds after srand(s):

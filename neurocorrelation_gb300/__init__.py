@@ -131,6 +131,7 @@ def load_library() -> ctypes.CDLL:
         "nc_set_input_rates": ([P, I32, P], I32), "nc_add_input_offset": ([P, I32, F], I32),
         "nc_set_detectors": ([P, I32, P, P], I32), "nc_get_detector_voltages": ([P, P, I32, P], I32),
         "nc_get_detector_voltage": ([P, I32, P], I32),
+        "nc_create_knn": ([I32, I32, F, ctypes.c_uint64, P, P, P], I32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -254,6 +255,24 @@ class NeuCor:
         for k, v in kw.items():
             setattr(self._params, k, v)
         self._materialize(xyz, pre, post, weight, length, inhibitory)
+        return self
+
+    @classmethod
+    def knn(cls, n: int, k: int, density: float = 8.0, seed: int = 1, params: Params | None = None, **kw):
+        """The network build_knn(n, k, density, seed) describes, built on the GPU
+        (nc_create_knn): identical to from_arrays(*build_knn(...)).  The kNN seed draws
+        the positions and weights; params.seed keys the simulation's own draws."""
+        self = cls(0, params=params)
+        for key, v in kw.items():
+            setattr(self._params, key, v)
+        xyz = np.zeros((int(n), 3), dtype=np.float32)
+        h = ctypes.c_void_p()
+        _check(self._lib.nc_create_knn(int(n), int(k), float(density), int(seed), ctypes.byref(self._params),
+                                       _p(xyz), ctypes.byref(h)))
+        self._h = h
+        self._xyz = xyz
+        self.n = int(n)
+        self.n_input_synapses = int(n) * int(k)
         return self
 
     def createNeuron(self, position):

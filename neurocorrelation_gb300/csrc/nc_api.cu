@@ -127,6 +127,7 @@ int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int
     nc::NetHost& h = net->host;
     std::vector<uint32_t>().swap(h.out_ringpos);
     std::vector<int32_t>().swap(h.csc_pre);
+    std::vector<int32_t>().swap(h.csc_post);
     std::vector<uint16_t>().swap(h.csc_dl);
     std::vector<float>().swap(h.w);
     std::vector<int64_t>().swap(h.in_ptr);
@@ -134,6 +135,86 @@ int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int
     *out = net;
     return NC_OK;
 }
+
+int nc_create_knn(int32_t n, int32_t k, float density, uint64_t seed, const nc_params* params, float* xyz_out,
+                  nc_net** out)
+{
+    if (!out || !params) return fail(NC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (n < 0 || k < 0 || !(density > 0.0f) || (n > 0 && k >= n)) return fail(NC_ERR_INVALID, "bad kNN shape");
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
+        return fail(NC_ERR_NODEVICE, "no CUDA device: the GB300 step has no CPU fallback");
+    nc_net* net = new (std::nothrow) nc_net();
+    if (!net) return fail(NC_ERR_NOMEM, "host allocation failed");
+    std::string err;
+    int rc = nc::build_knn_device(n, k, density, seed, *params, net, err);
+    if (rc == NC_ERR_UNSUPPORTED) {
+        // outside the device builder's capacities: the host builder, same network
+        delete net;
+        std::vector<float> xyz(3 * (size_t)n), w((size_t)n * k);
+        std::vector<int32_t> from((size_t)n * k), to((size_t)n * k);
+        rc = nc_build_knn(n, k, density, seed, xyz.data(), from.data(), to.data(), w.data());
+        if (rc != NC_OK) return fail(rc, "kNN build");
+        if (xyz_out) std::copy(xyz.begin(), xyz.end(), xyz_out);
+        return nc_create(n, xyz.data(), (int64_t)n * k, from.data(), to.data(), w.data(), nullptr, nullptr, params,
+                         out);
+    }
+    if (rc != NC_OK) {
+        delete net;
+        return fail(rc, err);
+    }
+    if (xyz_out) std::copy(net->host.xyz.begin(), net->host.xyz.end(), xyz_out);
+    std::vector<int64_t>().swap(net->host.in_ptr);
+    *out = net;
+    return NC_OK;
+}
+
+}  // extern "C"
+
+// The read-back tables of a network built on the device (creation order -> CSC
+// position, delays, inhibitory bits, out-synapse tables), fetched on first use.
+static int ensure_host_tables(nc_net* net)
+{
+    if (!net->dev_i2c) return NC_OK;
+    nc::NetHost& h = net->host;
+    const int64_t S = h.s;
+    const int32_t k = net->knn_k;
+    const auto& P = net->eng.P;
+    std::vector<int64_t> i2c((size_t)S);
+    std::vector<int32_t> to((size_t)S);
+    std::vector<uint16_t> dl((size_t)S);
+    NC_CALL(net->eng, download, i2c.data(), (const int64_t*)net->dev_i2c, (size_t)S);
+    NC_CALL(net->eng, download, to.data(), (const int32_t*)net->dev_to, (size_t)S);
+    NC_CALL(net->eng, download, (int16_t*)dl.data(), (const int16_t*)P.csc_dl, (size_t)S);
+    h.csc_delay.resize((size_t)S);
+    for (int64_t c = 0; c < S; ++c) h.csc_delay[(size_t)c] = dl[(size_t)c] & 0x3fff;
+    h.inh_bits.assign((size_t)((S + 31) / 32), 0u);  // U[0,1) weights: none inhibitory
+    // out-synapses of the source in slot s: its k in creation order
+    h.out_ptr.resize((size_t)h.n + 1);
+    for (int32_t s = 0; s <= h.n; ++s) h.out_ptr[(size_t)s] = (int64_t)s * k;
+    h.out_csc.resize((size_t)S);
+    h.out_post.resize((size_t)S);
+    h.out_delay.resize((size_t)S);
+    for (int32_t s = 0; s < h.n; ++s) {
+        const int32_t i = h.orig_id[(size_t)s];
+        for (int32_t m = 0; m < k; ++m) {
+            const int64_t e = (int64_t)i * k + m, q = (int64_t)s * k + m;
+            const int64_t c = i2c[(size_t)e];
+            h.out_csc[(size_t)q] = (int32_t)c;
+            h.out_post[(size_t)q] = h.slot_of[(size_t)to[(size_t)e]];
+            h.out_delay[(size_t)q] = (int16_t)dl[(size_t)c];
+        }
+    }
+    h.input_to_csc = std::move(i2c);
+    cudaFree(net->dev_i2c);
+    cudaFree(net->dev_to);
+    net->dev_i2c = nullptr;
+    net->dev_to = nullptr;
+    return NC_OK;
+}
+
+extern "C" {
 
 int nc_destroy(nc_net* net)
 {
@@ -494,6 +575,7 @@ int nc_read_last_fire(nc_net* net, float* out_n)
 int nc_read_weights(nc_net* net, float* out_s)
 {
     NC_NEED(net);
+    if (int rc = ensure_host_tables(net)) return rc;
     const nc::NetHost& h = net->host;
     if (!out_s && h.n_input) return fail(NC_ERR_INVALID, "null output");
     NC_CALL0(net->eng, flush_plasticity);
@@ -508,7 +590,9 @@ int nc_read_weights(nc_net* net, float* out_s)
 
 int nc_read_delays(nc_net* net, int32_t* out_s)
 {
-    if (!net || (!out_s && net->host.n_input)) return fail(NC_ERR_INVALID, "null argument");
+    NC_NEED(net);
+    if (!out_s && net->host.n_input) return fail(NC_ERR_INVALID, "null argument");
+    if (int rc = ensure_host_tables(net)) return rc;
     const nc::NetHost& h = net->host;
     for (int64_t k = 0; k < h.n_input; ++k) {
         const int64_t c = h.input_to_csc[(size_t)k];
@@ -519,7 +603,9 @@ int nc_read_delays(nc_net* net, int32_t* out_s)
 
 int nc_read_inhibitory(nc_net* net, uint8_t* out_s)
 {
-    if (!net || (!out_s && net->host.n_input)) return fail(NC_ERR_INVALID, "null argument");
+    NC_NEED(net);
+    if (!out_s && net->host.n_input) return fail(NC_ERR_INVALID, "null argument");
+    if (int rc = ensure_host_tables(net)) return rc;
     const nc::NetHost& h = net->host;
     for (int64_t k = 0; k < h.n_input; ++k) {
         const int64_t c = h.input_to_csc[(size_t)k];
@@ -536,6 +622,7 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
     *count = h.s;
     if (!out) return NC_OK;
     if (capacity < h.s) return fail(NC_ERR_INVALID, "snapshot buffer too small");
+    if (int rc = ensure_host_tables(net)) return rc;
     NC_CALL0(net->eng, flush_plasticity);
     const auto& sl = net->eng.slots[0];
     const auto& P = net->eng.P;

@@ -147,6 +147,18 @@ static bool grown_copy(int64_t m, int64_t size)
     return size > cap;
 }
 
+KnnGrid knn_grid(int32_t n, int32_t k, float density)
+{
+    KnnGrid G;
+    G.side = (float)std::cbrt((double)n / (double)density);
+    // uniform grid, cells of about k/8 points
+    const double cell_target = std::cbrt(std::max(1.0, (double)k / 8.0) / (double)density);
+    G.g = std::max(1, (int32_t)std::floor((double)G.side / cell_target));
+    G.g = std::min(G.g, 1024);
+    G.h = G.side / (float)G.g;
+    return G;
+}
+
 int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, const int32_t* to,
               const float* weight, const float* length, const uint8_t* inhibitory, const nc_params& p,
               NetHost& h, std::string& err)
@@ -337,10 +349,9 @@ int set_groups(NetHost& h, int32_t n_groups, const nc_group* groups, std::string
 // ------------------------------------------------------------------ C ABI
 namespace {
 thread_local std::string g_build_err;
-constexpr uint32_t kStreamPosition = 10u;
-constexpr uint32_t kStreamWeight = 11u;
-
-float unit24(uint32_t r) { return (float)(r >> 8) * 0x1p-24f; }
+using nc::kStreamPosition;
+using nc::kStreamWeight;
+using nc::unit24;
 
 struct Cand {
     float d;
@@ -363,7 +374,8 @@ extern "C" int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, 
         return NC_ERR_INVALID;
     if (n > 0 && k >= n) return NC_ERR_INVALID;
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    const float side = (float)std::cbrt((double)n / (double)density);
+    const nc::KnnGrid grid = nc::knn_grid(n, k, density);
+    const float side = grid.side;
     for (int32_t i = 0; i < n; ++i) {
         uint32_t o[4];
         nc_philox((uint32_t)i, 0u, kStreamPosition, 0u, k0, k1, o);
@@ -372,11 +384,8 @@ extern "C" int nc_build_knn(int32_t n, int32_t k, float density, uint64_t seed, 
         xyz[3 * (size_t)i + 2] = unit24(o[2]) * side;
     }
     if (k == 0 || n == 0) return NC_OK;
-    // uniform grid, cells of about k/8 points
-    const double cell_target = std::cbrt(std::max(1.0, (double)k / 8.0) / (double)density);
-    int32_t g = std::max(1, (int32_t)std::floor((double)side / cell_target));
-    g = std::min(g, 1024);
-    const float h = side / (float)g;
+    const int32_t g = grid.g;
+    const float h = grid.h;
     auto cell_of = [&](float v) { return std::min(g - 1, std::max(0, (int32_t)(v / h))); };
     std::vector<int32_t> cstart((size_t)g * g * g + 1, 0), cell((size_t)n);
     for (int32_t i = 0; i < n; ++i) {

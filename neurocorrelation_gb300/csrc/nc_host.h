@@ -68,6 +68,19 @@ void to_caller_order(const NetHost& h, const T* slots, T* out)
     for (int32_t i = 0; i < h.n; ++i) out[i] = slots[h.slot_of[(size_t)i]];
 }
 uint32_t rate_threshold(float rate_hz, float dt);
+
+// kNN networks (nc_build_knn, and its device counterpart in nc_build.cu): positions
+// uniform in a cube of side (n/density)^(1/3) from Philox stream kStreamPosition,
+// weights from kStreamWeight, neighbours searched over a uniform grid of g^3 cells.
+constexpr uint32_t kStreamPosition = 10u;
+constexpr uint32_t kStreamWeight = 11u;
+NC_HD inline float unit24(uint32_t r) { return (float)(r >> 8) * 0x1p-24f; }
+struct KnnGrid {
+    float side;
+    int32_t g;
+    float h;
+};
+KnnGrid knn_grid(int32_t n, int32_t k, float density);
 float ap_value(float x);                              // Neuron::AP, src/NeuCor.cpp:706-714
 float step_ms(int64_t k, float dt);                   // k steps as a float time difference
 

@@ -20,11 +20,25 @@ struct nc_net {
     std::vector<int32_t> det_near, det_ptr{0};
     int32_t* d_det = nullptr;      // det_near then det_ptr on the device
     float* d_volt = nullptr;
+    // built on the device (nc_create_knn): targets in creation order and the CSC position
+    // of every synapse, kept there until a read-back needs the host tables
+    int32_t* dev_to = nullptr;
+    int64_t* dev_i2c = nullptr;
+    int32_t knn_k = 0;
     ~nc_net()
     {
+        if (dev_to) cudaFree(dev_to);
+        if (dev_i2c) cudaFree(dev_i2c);
         if (d_raster) cudaFree(d_raster);
         if (d_raster_ids) cudaFree(d_raster_ids);
         if (d_det) cudaFree(d_det);
         if (d_volt) cudaFree(d_volt);
     }
 };
+
+namespace nc {
+// The kNN network of nc_build_knn built on the device into `net` (nc_build.cu);
+// NC_ERR_UNSUPPORTED when it exceeds the device builder's capacities.
+int build_knn_device(int32_t n, int32_t k, float density, uint64_t seed, const nc_params& p, nc_net* net,
+                     std::string& err);
+}  // namespace nc

@@ -88,7 +88,7 @@ void Engine::set_launch(const LaunchShape& shape, int ticks_per_graph)
 }
 
 int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err,
-                  const std::vector<int32_t>* horizons)
+                  const std::vector<int32_t>* horizons, bool device_synapses)
 {
     NC_CK(cudaGetDevice(&device));
     NC_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -237,6 +237,10 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         for (auto& v : inp) v += sl.syn_base;
         for (auto& v : outp) v += sl.syn_base;
         NC_CK(upload(P.in_ptr, inp, sl.ptr_base, stream));
+        if (dense && device_synapses) {
+            const int32_t chunks = (int32_t)((h.s + 31) / 32);
+            for (int32_t c = 0; c < chunks; c += NC_SPAN_CHUNKS) span_host.push_back(NcTile{(int32_t)q, c});
+        } else {
         NC_CK(upload(P.w, h.w, sl.syn_base, stream));
         NC_CK(upload(P.inh, h.inh_bits, sl.syn_base / 32, stream));
         std::vector<int32_t> never((size_t)h.s, NC_NEVER);
@@ -256,6 +260,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
             NC_CK(upload(P.out_csc, h.out_csc, sl.syn_base, stream));
             NC_CK(upload(P.out_delay, h.out_delay, sl.syn_base, stream));
             NC_CK(upload(P.out_ringpos, h.out_ringpos, sl.syn_base, stream));
+        }
         }
         NC_CK(upload(P.tables, h.tables, d.table_base, stream));
         if (!h.groups.empty()) NC_CK(upload(P.groups, h.groups, sl.group_base, stream));

@@ -29,8 +29,10 @@ public:
 
     // Packs the nets (all starting at step 1) and uploads them.  group_capacity is
     // the number of input-group entries reserved per net.
+    // device_synapses: the in-synapse streams (dense form) are written on the device by
+    // the caller (nc_build.cu); only the row starts come from the host description.
     int build(const std::vector<const NetHost*>& nets, int group_capacity, std::string& err,
-              const std::vector<int32_t>* horizons = nullptr);
+              const std::vector<int32_t>* horizons = nullptr, bool device_synapses = false);
     void set_launch(const LaunchShape& shape, int ticks_per_graph);
     // Runs `ticks` engine steps (every active net advances one step per tick).
     int step(int64_t ticks, std::string& err);

@@ -44,7 +44,6 @@ public:
         cap_ = cap;
         if (cap > 0) free_[0] = cap;
     }
-    int64_t capacity() const { return cap_; }
     int64_t alloc(int64_t len, int64_t align = 1)
     {
         if (len <= 0) return 0;
