@@ -345,6 +345,35 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
             "speedup_vs_one_at_a_time": (events / span) / (ev1 / span1)}
 
 
+def measure_large(G, mode, sim_steps=100, timed=5):
+    """The large single network: 2,000,000 neurons x 200 nearest targets (400M synapses),
+    2,000 inputs in 20 correlated groups at 10-40 Hz, STDP on, built on the device
+    (nc_create_knn), timed over a prefix of the 100,000-step horizon."""
+    n, k = 2_000_000, 200
+    rates = np.linspace(10.0, 40.0, 20)
+    groups = [dict(first=100 * g, count=100, rate_hz=float(rates[g]), correlated=1, jitter=2) for g in range(20)]
+    t0 = time.perf_counter()
+    net = G.NeuCor.knn(n, k, 8.0, seed=5, params=G.default_params(seed=5, step_mode=mode))
+    net.sync()
+    build_s = time.perf_counter() - t0
+    net.set_input_groups(groups)
+    net.run(3 * sim_steps)
+    st0 = net.stats()
+    ms, _ = net.time_steps(timed * sim_steps)
+    st1 = net.stats()
+    _, per = net.time_steps(20, per_kernel=True)
+    events = st1["launched"] - st0["launched"]
+    secs = ms / 1e3
+    st = timed * sim_steps
+    out = {"workload": "2M neurons x 200 nearest targets (400M synapses), 2,000 inputs in 20 correlated "
+                       "groups 10-40 Hz, STDP on", "steps_timed": st, "warmup_steps": 3 * sim_steps,
+           "device_build_s": build_s, "events_per_s": events / secs, "neuron_steps_per_s": n * st / secs,
+           "ms_per_sim_step": ms / st, "mean_rate_hz": (st1["fires"] - st0["fires"]) / (n * st / 1000.0),
+           "kernel_ms": per}
+    net.close()
+    return out
+
+
 def run_ours(args):
     world, rank, local = dist_env()
     pg = None
@@ -478,6 +507,8 @@ def run_ours(args):
         "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
     }
+    if world == 1 and args.large:
+        line["large_network"] = measure_large(G, mode)
     if world == 1 and args.forms:
         line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, mode),
                          "served": measure_served(G, args.served_requests, args.served_horizon_scale,
@@ -495,6 +526,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--large", action="store_true",
+                    help="also time the 2M x 200 network (built on the device) over a prefix")
     ap.add_argument("--step-mode", default="dense", choices=sorted(STEP_MODES),
                     help="form of the step kernels (results are the same in both)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
