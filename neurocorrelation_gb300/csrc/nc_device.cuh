@@ -28,12 +28,19 @@ static __device__ __forceinline__ uint32_t inh_bits32(const NcPools& P, int64_t 
     return __funnelshift_r(__ldg(P.inh + w0), __ldg(P.inh + w0 + 1), (uint32_t)(s & 31));
 }
 
+// The learning constants a kernel holds in registers (read from the descriptor once:
+// the descriptor lives in global memory, where every store could alias it).
+struct Rates {
+    float pre, post, lr;
+};
+static __device__ __forceinline__ Rates rates_of(const NcNetDesc& D) { return Rates{D.pre_factor, D.post_factor, D.lr}; }
+
 // Synapse::synapticPlasticity weight update and clamp (src/NeuCor.cpp:757-761);
 // fmin/fmax keep the C library's generic semantics.
-static __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const NcNetDesc& D)
+static __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const Rates& R)
 {
-    const float weightChange = D.pre_factor * traceS - D.post_factor * traceT;
-    float v = w + weightChange * D.lr;
+    const float weightChange = R.pre * traceS - R.post * traceT;
+    float v = w + weightChange * R.lr;
     if (!inh) {
         const float m = (v <= 1.0f) ? v : 1.0f;
         v = (m >= 0.0f) ? m : 0.0f;
@@ -42,6 +49,11 @@ static __device__ __forceinline__ float plasticity(float w, bool inh, float trac
         v = (m >= -1.0f) ? m : -1.0f;
     }
     return v;
+}
+
+static __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const NcNetDesc& D)
+{
+    return plasticity(w, inh, traceS, traceT, rates_of(D));
 }
 
 // RN32 of a double, returned as the (exactly representable) double: the 52-bit

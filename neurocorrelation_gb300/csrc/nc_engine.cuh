@@ -87,6 +87,7 @@ struct NcNetDesc {
     uint32_t* raster;     // device raster rows of n_words words
     unsigned long long* stats; // 4 counters: fires, launched, dropped, steps
     int64_t n_syn;        // synapses (the pool range is padded to a multiple of 32)
+    float tsum;           // NeuCor::currentTime after t-1 steps: the float sum of t-1 runSpeeds
 };
 
 struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8 chunks of

@@ -6,9 +6,10 @@
 // fire with no threshold and no refractory test.  In the stepped model the interval
 // after step t is evaluated once step t is complete (k_input_firers, launched after the
 // step's last kernel) and a fire inside it fires the near neurons at step t+1; the
-// schedule's float/double arithmetic is the reference's, so the reference's own
-// behaviour carries over, including that a period of a whole number of steps never
-// fires (its `currentT < fireTime` test excludes the boundary).
+// schedule's float/double arithmetic and its currentTime (the float sum of the steps'
+// runSpeeds) are the reference's, so the reference's own behaviour carries over,
+// including that with an exactly representable step a period of a whole number of steps
+// never fires (its `currentT < fireTime` test excludes the boundary).
 //
 // VoltageDetector::getVoltage (src/NeuCor.cpp:359-366): the mean potential of the
 // neurons closer than the detector's radius, summed in id order in float.
@@ -60,8 +61,9 @@ __global__ void k_input_firers(NcPools P)
     if (lane == 0) {
         float last = F.last;
         bool capped = false;
-        // the interval after the net's last completed step t = D.t - 1
-        const float currentT = __fmul_rn(__int2float_rn(D.t - 1), D.dt);
+        // the interval after the net's last completed step: its run call starts at the
+        // reference's accumulated currentTime
+        const float currentT = D.tsum;
         fired = firer_schedule(&last, D.dt, F.rate, currentT, &capped) ? 1 : 0;
         F.last = last;
         if (capped) atomicOr(P.dev_err, NC_DEV_ERR_FIRER_LOOP);

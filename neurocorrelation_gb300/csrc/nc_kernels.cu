@@ -430,6 +430,7 @@ __global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPo
                 if (D->stdp_done < D->t - 1) D->stdp_done = D->t - 1;
                 D->stats[3] += 1ull;
                 D->t += 1;
+                D->tsum = __fadd_rn(D->tsum, D->dt);  // currentTime = targetTime (src/NeuCor.cpp:616)
             }
         }
         if (threadIdx.x == 0) {

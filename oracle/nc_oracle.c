@@ -108,6 +108,8 @@ struct ncs_net {
     uint8_t* forced;      /* requests for step cur+1 (scheduledFireTime == T) */
     uint8_t* ufire;       /* InputFirer fires for step cur+1 (Neuron::fire, no threshold) */
     float* xyz;           /* neuron positions (NeuCor::positions) */
+    float tsum;           /* NeuCor::currentTime at the start of step cur's run call: the
+                             float sum of cur runSpeeds (NeuCor.cpp:616) */
 
     /* periodic input firers (InputFirer, NeuCor.cpp:305-345) */
     int32_t n_firers;
@@ -605,9 +607,10 @@ static int firer_schedule(float* last, float dt, float frequency, float currentT
     return fired;
 }
 
-static void firers_schedule(ncs_net* h, int32_t t)
+/* The interval after step `cur`, whose run call starts at NeuCor::currentTime = tsum. */
+static void firers_schedule(ncs_net* h)
 {
-    const float currentT = kdt(h, t);
+    const float currentT = h->tsum;
     for (int32_t i = 0; i < h->n_firers; ++i)
         if (firer_schedule(&h->f_last[i], h->dt, h->f_rate[i], currentT))
             for (int64_t k = h->f_ptr[i]; k < h->f_ptr[i + 1]; ++k) h->ufire[h->f_ids[k]] = 1;
@@ -634,7 +637,7 @@ int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* x
             if (get_dist(&h->xyz[3 * (int64_t)j], &xyz[3 * (int64_t)i]) < radius[i]) h->f_ids[total++] = j;
         h->f_ptr[i + 1] = total;
     }
-    firers_schedule(h, h->cur);
+    firers_schedule(h);
     return 0;
 }
 
@@ -642,7 +645,7 @@ int ncs_set_firer_rates(ncs_net* h, int32_t count, const float* rates)
 {
     if (!h || count < 0 || count > h->n_firers) return -1;
     for (int32_t i = 0; i < count; ++i) h->f_rate[i] = rates[i];
-    firers_schedule(h, h->cur);
+    firers_schedule(h);
     return 0;
 }
 
@@ -651,7 +654,7 @@ int ncs_add_firer_offset(ncs_net* h, int32_t id, float t)
 {
     if (!h || id < 0 || id >= h->n_firers) return -1;
     h->f_last[id] += t;
-    firers_schedule(h, h->cur);
+    firers_schedule(h);
     return 0;
 }
 
@@ -678,8 +681,10 @@ int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
         /* background fires for step t+1, NeuCor.cpp:604-607 */
         memset(h->forced, 0, (size_t)h->n);
         if (h->p.background_firing && h->n > 0) draw_background(h, t);
-        /* input firers schedule the interval after t (NeuCor.cpp:599-602) */
-        firers_schedule(h, t);
+        /* input firers schedule the interval after t (NeuCor.cpp:599-602), at the
+         * reference's accumulated time of step t (currentTime = targetTime, :616) */
+        h->tsum = h->tsum + h->dt;
+        firers_schedule(h);
         if (raster) {
             uint8_t* rr = raster + (int64_t)r * row;
             memset(rr, 0, (size_t)row);

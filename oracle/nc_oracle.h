@@ -92,10 +92,11 @@ int ncs_set_rates(ncs_net* h, float learning_rate, float pre_factor, float post_
 int ncs_schedule_fire(ncs_net* h, int32_t n, const int32_t* ids);
 /* Periodic input firers (NeuCor::setInputRateArray, InputFirer, NeuCor.cpp:46-64,
  * 305-345): firer i at xyz[3i..] fires every neuron closer than radius[i] at the
- * reference's schedule for rates[i] Hz.  A fire time in (t*dt, (t+1)*dt) fires those
- * neurons at step t+1, without threshold or refractory test (Neuron::fire).  Each
- * change evaluates the interval after the current step at once; every step then
- * evaluates the next one. */
+ * reference's schedule for rates[i] Hz.  The interval after step t runs from the
+ * reference's currentTime T_t (the float sum of t runSpeeds) to T_t + runSpeed; a fire
+ * time inside it fires those neurons at step t+1, without threshold or refractory test
+ * (Neuron::fire).  Each change evaluates the interval after the current step at once;
+ * every step then evaluates the next one. */
 int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* xyz, const float* radius);
 int ncs_set_firer_rates(ncs_net* h, int32_t count, const float* rates);
 int ncs_add_firer_offset(ncs_net* h, int32_t id, float t);
