@@ -157,13 +157,14 @@ int nc_set_input_groups(nc_net* net, int32_t n_groups, const nc_group* groups);
  * NULL: a random position from the C library's rand(), as the reference, and radius
  * 1).  rates_hz[i] is firer i's frequency (the reference re-reads its borrowed array
  * every run; here the rates are copied: change them with nc_set_input_rates).  Each
- * firer keeps the reference's schedule (lastFire + k*1000/f, float/double arithmetic,
- * currentTime the float sum of the steps' run_speed); a fire time inside the interval
- * after step t fires every neuron closer than the radius at step t+1 with Neuron::fire's
- * semantics (no threshold or refractory test).  Like the reference, with an exactly
- * representable run_speed a period of a whole number of steps never fires unless
- * shifted with nc_add_input_offset.  Every change evaluates the interval after the last
- * completed step at once. */
+ * firer keeps the reference's schedule (lastFire + k*1000/f, float/double arithmetic):
+ * step t evaluates it for the run call at currentTime T_t, the float sum of t
+ * run_speeds, and a fire time inside (T_t, T_t + run_speed) fires every neuron closer
+ * than the radius at step t+1 with Neuron::fire's semantics (no threshold or refractory
+ * test); a firer set before the first step also meets the call at time 0, whose fires
+ * land in step 1.  Changes take effect at the next step, as they do at the next run in
+ * the reference.  Like the reference, with an exactly representable run_speed a period
+ * of a whole number of steps never fires unless shifted with nc_add_input_offset. */
 int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
                             const float* radius);
 /* New frequencies of the first `count` firers (the reference's borrowed rate array). */

@@ -255,6 +255,8 @@ static int upload_firers(nc_net* net, const std::vector<NcFirer>& old, const std
     for (size_t i = 0; i < f.size(); ++i) {
         f[i].net = 0;
         f[i].last = i < old.size() ? old[i].last : 0.0f;  // InputFirer: lastFire(0.0)
+        // a firer made before the first step also meets the run call at time 0
+        f[i].first = i < old.size() ? old[i].first : (net->step == 0 ? 1 : 0);
         f[i].rate = i < rates.size() ? rates[i] : 0.0f;
         f[i].near_begin = (int32_t)near.size();
         for (int32_t id : net->firer_near[i]) near.push_back(net->host.slot_of[(size_t)id]);

@@ -95,7 +95,7 @@ struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8
     int32_t first;       // local id of the first neuron (multiple of 32), or first chunk
 };
 
-constexpr int NC_SPAN_CHUNKS = 8;
+constexpr int NC_SPAN_CHUNKS = 8;  // 32-synapse chunks per span of the dense synapse pass
 
 struct NcFirer {         // periodic input firer (InputFirer, src/NeuCor.cpp:305-345)
     int32_t net;
@@ -103,7 +103,8 @@ struct NcFirer {         // periodic input firer (InputFirer, src/NeuCor.cpp:305
     float rate;          // its entry of the rate array, Hz
     int32_t near_begin;  // neuron slots firer_near[near_begin .. near_end)
     int32_t near_end;
-};  // 32-synapse chunks per span of the dense synapse pass
+    int32_t first;       // set before the net's first step: the run call at time 0 evaluates it too
+};
 
 struct NcPools {
     // neurons
@@ -229,8 +230,9 @@ int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);
-// Input firers (nc_inputs.cu): each firer's schedule for the interval after the last
-// completed step of its net; fires land in that net's ufire bits of the next step.
+// Input firers (nc_inputs.cu), launched before a step's kernels: each firer's schedule
+// for the run call that starts at its net's step t; fires land in the ufire bits of
+// step t+1 (and, before the first step, those of the time-0 call in step 1's).
 int launch_input_firers(const NcPools& P, void* stream);
 // Mean potential of each detector's near neurons (caller ids; near_ptr has count+1 entries).
 int launch_detector_voltages(const NcPools& P, int32_t neuron_base, const int32_t* near, const int32_t* near_ptr,

@@ -3,11 +3,13 @@
 // InputFirer (src/NeuCor.cpp:305-345): at every NeuCor::run the firer schedules the fire
 // times lastFire + k*1000/frequency that fall in (currentT, currentT + runSpeed), and
 // when one comes up it calls Neuron::fire() on every neuron closer than its radius — a
-// fire with no threshold and no refractory test.  In the stepped model the interval
-// after step t is evaluated once step t is complete (k_input_firers, launched after the
-// step's last kernel) and a fire inside it fires the near neurons at step t+1; the
-// schedule's float/double arithmetic and its currentTime (the float sum of the steps'
-// runSpeeds) are the reference's, so the reference's own behaviour carries over,
+// fire with no threshold and no refractory test.  In the stepped model step t is the
+// run call that starts at currentTime T_t (the float sum of t runSpeeds, as the
+// reference keeps it): k_input_firers runs that call's schedule before the step's
+// kernels — after any change the caller made before it, as in the reference — and a
+// fire inside (T_t, T_t + runSpeed) fires the near neurons at step t+1.  Before the
+// first step it also runs the call at time 0, whose fires land in step 1.  The
+// schedule's float/double arithmetic is the reference's, so its behaviour carries over,
 // including that with an exactly representable step a period of a whole number of steps
 // never fires (its `currentT < fireTime` test excludes the boundary).
 //
@@ -48,7 +50,16 @@ __device__ bool firer_schedule(float* last, float dt, float frequency, float cur
     return fired;
 }
 
-// Warp per firer: lane 0 runs the schedule, the warp marks the near neurons.
+__device__ void mark_near(const NcPools& P, const NcFirer& F, uint32_t* uf, int lane)
+{
+    for (int32_t k = F.near_begin + lane; k < F.near_end; k += 32) {
+        const int32_t slot = P.firer_near[k];
+        atomicOr(uf + (slot >> 5), 1u << (slot & 31));
+    }
+}
+
+// Warp per firer, before the kernels of its net's step t = D.t: lane 0 runs the
+// schedule, the warp marks the near neurons.
 __global__ void k_input_firers(NcPools P)
 {
     const int lane = threadIdx.x & 31;
@@ -56,25 +67,24 @@ __global__ void k_input_firers(NcPools P)
     if (f >= P.n_firers) return;
     NcFirer& F = P.firers[f];
     const NcNetDesc& D = P.nets[F.net];
-    if (!D.active) return;
-    int fired = 0;
+    if (!D.active || D.t > D.t_end) return;
+    int fired0 = 0, fired = 0;
     if (lane == 0) {
         float last = F.last;
-        bool capped = false;
-        // the interval after the net's last completed step: its run call starts at the
-        // reference's accumulated currentTime
-        const float currentT = D.tsum;
-        fired = firer_schedule(&last, D.dt, F.rate, currentT, &capped) ? 1 : 0;
+        bool capped = false, capped0 = false;
+        // the run call at time 0 (D.tsum = 0 before the first step): fires at step 1
+        if (F.first && D.t == 1) fired0 = firer_schedule(&last, D.dt, F.rate, D.tsum, &capped0) ? 1 : 0;
+        // the call starting at T_t = T_{t-1} + runSpeed (currentTime = targetTime)
+        fired = firer_schedule(&last, D.dt, F.rate, __fadd_rn(D.tsum, D.dt), &capped) ? 1 : 0;
         F.last = last;
-        if (capped) atomicOr(P.dev_err, NC_DEV_ERR_FIRER_LOOP);
+        F.first = 0;
+        if (capped || capped0) atomicOr(P.dev_err, NC_DEV_ERR_FIRER_LOOP);
     }
+    fired0 = __shfl_sync(kFull, fired0, 0);
     fired = __shfl_sync(kFull, fired, 0);
-    if (!fired) return;
-    uint32_t* uf = P.ufire + (int64_t)(D.t & 1) * P.total_words + D.word_base;
-    for (int32_t k = F.near_begin + lane; k < F.near_end; k += 32) {
-        const int32_t slot = P.firer_near[k];
-        atomicOr(uf + (slot >> 5), 1u << (slot & 31));
-    }
+    uint32_t* uf = P.ufire + D.word_base;
+    if (fired0) mark_near(P, F, uf + (int64_t)(D.t & 1) * P.total_words, lane);
+    if (fired) mark_near(P, F, uf + (int64_t)((D.t + 1) & 1) * P.total_words, lane);
 }
 
 // Thread per detector: mean potential of its near neurons (caller ids, ascending).

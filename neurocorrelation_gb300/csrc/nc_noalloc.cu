@@ -68,7 +68,7 @@ extern "C" int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream)
         // the dense form keeps no scratch between its launches: the network's own arrays
         // are all it reads and writes
         for (int32_t k = 0; k < n_steps; ++k)
-            if (nc::launch_step_dense(net->eng.P, net->eng.L, s) || nc::launch_input_firers(net->eng.P, s))
+            if (nc::launch_input_firers(net->eng.P, s) || nc::launch_step_dense(net->eng.P, net->eng.L, s))
                 return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("nc_run_noalloc launch", cudaGetLastError()));
     } else {
         const int64_t neurons = net->eng.P.fired_cap;
@@ -91,8 +91,8 @@ extern "C" int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream)
         if (e != cudaSuccess)
             return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("cudaMemsetAsync(noalloc counters)", e));
         for (int32_t k = 0; k < n_steps; ++k) {
-            if (nc::launch_neuron_step(P, net->eng.L, s) || nc::launch_spike_launch(P, net->eng.L, s) ||
-                nc::launch_input_firers(P, s))
+            if (nc::launch_input_firers(P, s) || nc::launch_neuron_step(P, net->eng.L, s) ||
+                nc::launch_spike_launch(P, net->eng.L, s))
                 return nc::set_last_error(NC_ERR_CUDA, nc::cuda_msg("nc_run_noalloc launch", cudaGetLastError()));
         }
     }

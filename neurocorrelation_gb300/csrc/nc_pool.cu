@@ -335,8 +335,8 @@ int Engine::step(int64_t ticks, std::string& err)
 
 int Engine::launch_tick(cudaStream_t s)
 {
-    int rc = dense ? launch_step_dense(P, L, s) : (launch_neuron_step(P, L, s) | launch_spike_launch(P, L, s));
-    if (P.n_firers > 0) rc |= launch_input_firers(P, s);
+    int rc = P.n_firers > 0 ? launch_input_firers(P, s) : 0;  // the step's run-call schedule first
+    rc |= dense ? launch_step_dense(P, L, s) : (launch_neuron_step(P, L, s) | launch_spike_launch(P, L, s));
     return rc;
 }
 
@@ -360,15 +360,6 @@ int Engine::set_firers(const std::vector<NcFirer>& firers, const std::vector<int
     P.firers = (NcFirer*)firers_buf_;
     P.firer_near = (int32_t*)near_buf_;
     P.n_firers = (int32_t)firers.size();
-    return evaluate_firers(err);
-}
-
-int Engine::evaluate_firers(std::string& err)
-{
-    if (launch_input_firers(P, stream)) {
-        err = cuda_msg("input firers", cudaGetLastError());
-        return NC_ERR_CUDA;
-    }
     NC_CK(cudaStreamSynchronize(stream));
     return NC_OK;
 }
@@ -390,7 +381,8 @@ int Engine::write_firers(const std::vector<NcFirer>& in, std::string& err)
     }
     if (P.n_firers == 0) return NC_OK;
     NC_CK(cudaMemcpyAsync(P.firers, in.data(), sizeof(NcFirer) * in.size(), cudaMemcpyHostToDevice, stream));
-    return evaluate_firers(err);
+    NC_CK(cudaStreamSynchronize(stream));
+    return NC_OK;
 }
 
 int Engine::step_timed(int64_t ticks, float* ms, std::string& err)
@@ -415,6 +407,10 @@ int Engine::time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::str
     std::vector<cudaEvent_t> ev(3 * (size_t)std::max(ticks, 0));
     for (auto& e : ev) NC_CK(cudaEventCreate(&e));
     for (int k = 0; k < ticks; ++k) {
+        if (P.n_firers > 0 && launch_input_firers(P, stream)) {
+            err = "launch";
+            return NC_ERR_CUDA;
+        }
         NC_CK(cudaEventRecord(ev[3 * k], stream));
         if (dense ? launch_dense_synapses(P, L, stream) : launch_neuron_step(P, L, stream)) {
             err = "launch";
@@ -426,10 +422,6 @@ int Engine::time_kernels(int ticks, float* neuron_ms, float* launch_ms, std::str
             return NC_ERR_CUDA;
         }
         NC_CK(cudaEventRecord(ev[3 * k + 2], stream));
-        if (P.n_firers > 0 && launch_input_firers(P, stream)) {
-            err = "launch";
-            return NC_ERR_CUDA;
-        }
     }
     NC_CK(cudaStreamSynchronize(stream));
     double sa = 0, sb = 0;

@@ -65,8 +65,8 @@ public:
     // Launches one tick of the engine's form on `s` (no graph), the input firers' schedule
     // included.
     int launch_tick(cudaStream_t s);
-    // Periodic input firers (replaces the set), their state read and written back; every
-    // change evaluates the interval after the last completed step at once.
+    // Periodic input firers (replaces the set), their state read and written back; the
+    // next step's run-call schedule sees every change.
     int set_firers(const std::vector<NcFirer>& firers, const std::vector<int32_t>& near, std::string& err);
     int read_firers(std::vector<NcFirer>& out, std::string& err);
     int write_firers(const std::vector<NcFirer>& in, std::string& err);
@@ -78,7 +78,6 @@ private:
     T* alloc(size_t count, std::string& err);
     std::vector<void*> allocs_;
     cudaGraphExec_t graph_ = nullptr;
-    int evaluate_firers(std::string& err);
     void* firers_buf_ = nullptr;
     void* near_buf_ = nullptr;
     int32_t* d_ids_ = nullptr;

@@ -107,6 +107,7 @@ struct ncs_net {
     int32_t* busy;        /* in-synapses not FREE, to skip idle neurons */
     uint8_t* forced;      /* requests for step cur+1 (scheduledFireTime == T) */
     uint8_t* ufire;       /* InputFirer fires for step cur+1 (Neuron::fire, no threshold) */
+    uint8_t* ufire_next;  /* ... for step cur+2 */
     float* xyz;           /* neuron positions (NeuCor::positions) */
     float tsum;           /* NeuCor::currentTime at the start of step cur's run call: the
                              float sum of cur runSpeeds (NeuCor.cpp:616) */
@@ -116,6 +117,7 @@ struct ncs_net {
     float* f_last;        /* InputFirer::lastFire, ms */
     float* f_rate;        /* the firer's entry of the rate array, Hz */
     int64_t* f_ptr;       /* near lists: f_ids[f_ptr[i] .. f_ptr[i+1]) */
+    uint8_t* f_first;     /* set before the first step: the run call at time 0 evaluates it too */
     int32_t* f_ids;
 
     /* arrivals bucketed by step modulo ring */
@@ -311,6 +313,7 @@ ncs_net* ncs_create(int32_t n, const float* xyz, int64_t n_syn, const int32_t* s
     h->busy = (int32_t*)xcalloc((size_t)n, sizeof(int32_t));
     h->forced = (uint8_t*)xcalloc((size_t)n, 1);
     h->ufire = (uint8_t*)xcalloc((size_t)n, 1);
+    h->ufire_next = (uint8_t*)xcalloc((size_t)n, 1);
     for (int32_t j = 0; j < n; ++j) {
         h->pot[j] = -70.0f;   /* setPotential(baselevel) */
         h->activity[j] = 0.0f;
@@ -340,8 +343,8 @@ void ncs_destroy(ncs_net* h)
     free(h->out_syn); free(h->input_to_csc); free(h->w); free(h->inh); free(h->depol);
     free(h->arr); free(h->t_arr); free(h->launch_step); free(h->stdp_step);
     free(h->pot); free(h->activity); free(h->lf); free(h->firings); free(h->act_start);
-    free(h->busy); free(h->forced); free(h->ufire);
-    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids); free(h->xyz);
+    free(h->busy); free(h->forced); free(h->ufire); free(h->ufire_next);
+    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids); free(h->f_first); free(h->xyz);
     if (h->bucket)
         for (int32_t r = 0; r < h->ring; ++r) free(h->bucket[r]);
     free(h->bucket); free(h->bucket_len); free(h->bucket_cap);
@@ -607,21 +610,33 @@ static int firer_schedule(float* last, float dt, float frequency, float currentT
     return fired;
 }
 
-/* The interval after step `cur`, whose run call starts at NeuCor::currentTime = tsum. */
-static void firers_schedule(ncs_net* h)
+/* The firers' schedule for the run call starting at currentT (NeuCor::run, NeuCor.cpp:
+ * 599-602); fires go to `mark` (the step after that call's neuron updates). */
+static void firers_schedule(ncs_net* h, float currentT, int first_only, uint8_t* mark)
 {
-    const float currentT = h->tsum;
-    for (int32_t i = 0; i < h->n_firers; ++i)
+    for (int32_t i = 0; i < h->n_firers; ++i) {
+        if (first_only && !h->f_first[i]) continue;
         if (firer_schedule(&h->f_last[i], h->dt, h->f_rate[i], currentT))
-            for (int64_t k = h->f_ptr[i]; k < h->f_ptr[i + 1]; ++k) h->ufire[h->f_ids[k]] = 1;
+            for (int64_t k = h->f_ptr[i]; k < h->f_ptr[i + 1]; ++k) mark[h->f_ids[k]] = 1;
+    }
 }
 
 int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* xyz, const float* radius)
 {
     if (!h || count < 0 || (count > 0 && (!xyz || !radius))) return -1;
-    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids);
+    /* the first min(old, count) firers keep their state: setInputRateArray appends or
+       pops at the end (NeuCor.cpp:46-64) */
+    const int32_t keep = h->n_firers < count ? h->n_firers : count;
+    uint8_t* first = (uint8_t*)xcalloc((size_t)count, 1);
+    float* last = (float*)xcalloc((size_t)count, sizeof(float));  /* lastFire(0.0), NeuCor.cpp:311 */
+    for (int32_t i = 0; i < count; ++i) {
+        first[i] = i < keep ? h->f_first[i] : (uint8_t)(h->cur == 0);
+        last[i] = i < keep ? h->f_last[i] : 0.0f;
+    }
+    free(h->f_last); free(h->f_rate); free(h->f_ptr); free(h->f_ids); free(h->f_first);
     h->n_firers = count;
-    h->f_last = (float*)xcalloc((size_t)count, sizeof(float));  /* lastFire(0.0), NeuCor.cpp:311 */
+    h->f_first = first;
+    h->f_last = last;
     h->f_rate = (float*)xcalloc((size_t)count, sizeof(float));
     h->f_ptr = (int64_t*)xcalloc((size_t)count + 1, sizeof(int64_t));
     int64_t total = 0;
@@ -637,7 +652,6 @@ int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* x
             if (get_dist(&h->xyz[3 * (int64_t)j], &xyz[3 * (int64_t)i]) < radius[i]) h->f_ids[total++] = j;
         h->f_ptr[i + 1] = total;
     }
-    firers_schedule(h);
     return 0;
 }
 
@@ -645,7 +659,6 @@ int ncs_set_firer_rates(ncs_net* h, int32_t count, const float* rates)
 {
     if (!h || count < 0 || count > h->n_firers) return -1;
     for (int32_t i = 0; i < count; ++i) h->f_rate[i] = rates[i];
-    firers_schedule(h);
     return 0;
 }
 
@@ -654,8 +667,13 @@ int ncs_add_firer_offset(ncs_net* h, int32_t id, float t)
 {
     if (!h || id < 0 || id >= h->n_firers) return -1;
     h->f_last[id] += t;
-    firers_schedule(h);
     return 0;
+}
+
+int32_t ncs_n_firers(const ncs_net* h) { return h ? h->n_firers : 0; }
+void ncs_read_firer_last(const ncs_net* h, float* out)
+{
+    memcpy(out, h->f_last, sizeof(float) * (size_t)h->n_firers);
 }
 
 int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
@@ -664,11 +682,20 @@ int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
     const int64_t row = ((int64_t)h->n + 7) / 8;
     for (int32_t r = 0; r < n_steps; ++r) {
         int32_t t = h->cur + 1;
+        /* the input firers' run calls: the one at time 0 before the first step (its fires
+         * land at step 1), then the one starting at T_t (fires at step t+1), each at the
+         * reference's accumulated currentTime (NeuCor.cpp:599-602, 616) */
+        if (h->n_firers > 0) {
+            if (t == 1) firers_schedule(h, h->tsum, 1, h->ufire);
+            for (int32_t i = 0; i < h->n_firers; ++i) h->f_first[i] = 0;
+            firers_schedule(h, h->tsum + h->dt, 0, h->ufire_next);
+        }
         for (int32_t j = 0; j < h->n; ++j) {
             int forced = h->forced[j] || input_request(h, j, t);
             neuron_run(h, j, t, forced, h->ufire[j]);
         }
-        memset(h->ufire, 0, (size_t)h->n);
+        { uint8_t* u = h->ufire; h->ufire = h->ufire_next; h->ufire_next = u; }
+        memset(h->ufire_next, 0, (size_t)h->n);
         /* spikes arriving at T: Synapse::run, NeuCor.cpp:718-726 */
         int32_t slot = t & (h->ring - 1);
         for (int64_t q = 0; q < h->bucket_len[slot]; ++q) {
@@ -681,10 +708,7 @@ int ncs_run(ncs_net* h, int32_t n_steps, uint8_t* raster, float* pot_trace)
         /* background fires for step t+1, NeuCor.cpp:604-607 */
         memset(h->forced, 0, (size_t)h->n);
         if (h->p.background_firing && h->n > 0) draw_background(h, t);
-        /* input firers schedule the interval after t (NeuCor.cpp:599-602), at the
-         * reference's accumulated time of step t (currentTime = targetTime, :616) */
-        h->tsum = h->tsum + h->dt;
-        firers_schedule(h);
+        h->tsum = h->tsum + h->dt;  /* currentTime = targetTime (NeuCor.cpp:616) */
         if (raster) {
             uint8_t* rr = raster + (int64_t)r * row;
             memset(rr, 0, (size_t)row);

@@ -92,14 +92,18 @@ int ncs_set_rates(ncs_net* h, float learning_rate, float pre_factor, float post_
 int ncs_schedule_fire(ncs_net* h, int32_t n, const int32_t* ids);
 /* Periodic input firers (NeuCor::setInputRateArray, InputFirer, NeuCor.cpp:46-64,
  * 305-345): firer i at xyz[3i..] fires every neuron closer than radius[i] at the
- * reference's schedule for rates[i] Hz.  The interval after step t runs from the
- * reference's currentTime T_t (the float sum of t runSpeeds) to T_t + runSpeed; a fire
- * time inside it fires those neurons at step t+1, without threshold or refractory test
- * (Neuron::fire).  Each change evaluates the interval after the current step at once;
- * every step then evaluates the next one. */
+ * reference's schedule for rates[i] Hz.  At its start step t evaluates the run call at
+ * the reference's currentTime T_t (the float sum of t runSpeeds): a fire time inside
+ * (T_t, T_t + runSpeed) fires those neurons at step t+1, without threshold or
+ * refractory test (Neuron::fire).  Step 1 also evaluates the call at time 0 for the
+ * firers set before it, whose fires land in step 1.  Changes are seen by the next step.
+ * xyz and radius give all `count` firers; the first min(previous, count) keep their
+ * state (setInputRateArray appends and pops at the end). */
 int ncs_set_firers(ncs_net* h, int32_t count, const float* rates, const float* xyz, const float* radius);
 int ncs_set_firer_rates(ncs_net* h, int32_t count, const float* rates);
 int ncs_add_firer_offset(ncs_net* h, int32_t id, float t);
+int32_t ncs_n_firers(const ncs_net* h);
+void ncs_read_firer_last(const ncs_net* h, float* out);  /* InputFirer::lastFire, ms */
 
 /* Runs n steps.  raster (may be NULL): n * ceil(N/8) bytes, bit j of row r set
  * when neuron j fired at step cur+1+r.  pot_trace (may be NULL): n * N floats. */

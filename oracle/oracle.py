@@ -91,6 +91,9 @@ def lib() -> ctypes.CDLL:
         L.ncs_set_firers.argtypes = [P, ctypes.c_int32, P, P, P]
         L.ncs_set_firer_rates.argtypes = [P, ctypes.c_int32, P]
         L.ncs_add_firer_offset.argtypes = [P, ctypes.c_int32, ctypes.c_float]
+        L.ncs_n_firers.restype = ctypes.c_int32
+        L.ncs_n_firers.argtypes = [P]
+        L.ncs_read_firer_last.argtypes = [P, P]
         L.ncs_run.argtypes = [P, ctypes.c_int32, P, P]
         L.ncs_step.restype = ctypes.c_int32
         L.ncs_step.argtypes = [P]
@@ -189,6 +192,12 @@ class OracleS:
     def add_firer_offset(self, firer: int, t_ms: float):
         """NeuCor::addInputOffset."""
         assert lib().ncs_add_firer_offset(self.h, int(firer), float(t_ms)) == 0
+
+    def firer_last(self):
+        """InputFirer::lastFire of every firer."""
+        out = np.zeros(lib().ncs_n_firers(self.h), dtype=np.float32)
+        lib().ncs_read_firer_last(self.h, _ptr(out))
+        return out
 
     def set_rates(self, learning_rate, pre_factor, post_factor):
         lib().ncs_set_rates(self.h, learning_rate, pre_factor, post_factor)
@@ -325,9 +334,12 @@ def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps
     fin = np.frombuffer(data, dtype=np.float32, count=3 * n, offset=off)
     off += 12 * n
     inh = np.frombuffer(data, dtype=np.uint8, count=s, offset=off)
+    off += s
+    nf = len(firers)
+    flast = np.frombuffer(data, dtype=np.float32, count=nf * steps, offset=off).reshape(steps, nf)
     return {"raster": raster.copy(), "pots": None if pots is None else pots.copy(), "weights": ckw.copy(),
             "pot": fin[:n].copy(), "activity": fin[n:2 * n].copy(), "last_fire": fin[2 * n:].copy(),
-            "inhibitory": inh.copy()}
+            "inhibitory": inh.copy(), "firer_last": flast.copy()}
 
 
 def reference_construct(n: int, seed: int):

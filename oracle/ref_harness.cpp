@@ -178,6 +178,7 @@ public:
         std::vector<float> pots;
         if (sc_.record_pot) pots.resize((size_t)n * sc_.steps);
         std::vector<float> ckw;
+        std::vector<float> firer_last;  // InputFirer::lastFire of every firer after each run call
         std::vector<uint8_t> hit(n);
         std::vector<int32_t> target(n), ids(n > 0 ? n : 1);
         size_t ck = 0;
@@ -217,6 +218,7 @@ public:
                     for (auto& neu : brain_->neurons) neu.run();
                 }
             }
+            for (auto& firer : brain_->inputHandler) firer_last.push_back(firer.lastFire);
             const float T = brain_->currentTime;
             uint8_t* rr = &raster[row * (size_t)(t - 1)];
             for (int32_t j = 0; j < n; ++j) {
@@ -248,6 +250,7 @@ public:
             inh[k] = syn && syn->inhibitory ? 1 : 0;
         }
         fwrite(inh.data(), 1, inh.size(), out);
+        fwrite(firer_last.data(), sizeof(float), firer_last.size(), out);
         fclose(out);
         delete brain_;
         return 0;

@@ -88,6 +88,24 @@ def main():
     save("native_knn200", xyz=xyz, pre=pre, post=post, w=w, groups=groups_arr(g4), steps=np.asarray(1000),
          raster=r["raster"], inhibitory=r["inhibitory"], pots_every50=r["pots"][49::50], **{"p_" + k: v for k, v in params_dict(p4).items()})
 
+    # E. InputFirer's schedule through the reference's own run calls: lastFire of every
+    # firer after each call, at steps that are and are not exactly representable
+    rates = np.array([50.0, 33.3, 125.0, 700.0, 2500.0, 0.0, 20.0], np.float32)
+    offsets = [0.0, 2.0, -2.0, 0.37, 0.0, 1.0, 0.25]
+    xyz = np.array([[0, 0, 0], [0.3, 0.3, 0], [0.3, -0.3, 0]], np.float32)
+    pre, post, w = np.array([0, 0], np.int32), np.array([1, 2], np.int32), np.array([0.5, 0.5], np.float32)
+    fdts, flasts = [], []
+    for dt in (0.02, 0.1, 0.25, 0.3, 1.0, 2.0):
+        fr = [dict(pos=(0.0, 0.0, 0.0), radius=0.1, rate_hz=float(rates[i]), offset_ms=offsets[i])
+              for i in range(len(rates))]
+        steps = int(round(60.0 / dt))
+        r = O.run_reference("continuous", xyz, pre, post, w, O.default_params(run_speed=dt, seed=1), steps=steps,
+                            firers=fr)
+        fdts.append(dt)
+        flasts.append(r["firer_last"])
+    save("firer_schedule", dts=np.asarray(fdts, np.float32), rates=rates, offsets=np.asarray(offsets, np.float32),
+         steps=np.asarray([x.shape[0] for x in flasts], np.int32), last=np.concatenate(flasts))
+
     # D. the reference constructor NeuCor(60) after srand(3)
     xyz, fr, to, w, ln = O.reference_construct(60, 3)
     save("construct_n60_seed3", xyz=xyz, pre=fr, post=to, w=w, length=ln)

@@ -2,8 +2,10 @@
 voltage detectors (NeuCor::setDetectors / getDetectorVoltage) through the C ABI.
 
 Firers: the GPU against the oracle's restatement of InputFirer::schedule (the reference's
-float/double arithmetic; a fire time in (t*dt, (t+1)*dt) fires the near neurons at step
-t+1 without threshold or refractory test), bit for bit, in both forms of the step.
+float/double arithmetic on its accumulated currentTime T_t; a fire time in
+(T_t, T_t + dt) fires the near neurons at step t+1 without threshold or refractory test),
+bit for bit, in both forms of the step, with changes between runs: offsets, rates, firers
+appended and popped, and offsets set before the first step (the FEW_NEURONS pattern).
 Detectors: the mean potential of the neurons within the radius, summed in id order in
 float, against the same sum over the potentials read back."""
 import numpy as np
@@ -21,32 +23,42 @@ def bits(a):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_periodic_firers_match_oracle(nc, oracle_mod, mode):
+@pytest.mark.parametrize("dt,scale", [(1.0, 1.0), (0.02, 25.0), (0.3, 4.0)])
+def test_periodic_firers_match_oracle(nc, oracle_mod, mode, dt, scale):
     G, O = nc, oracle_mod
     xyz, pre, post, w = knn_net(400, 10, 61, inhibitory=0.1)
-    pkw = dict(seed=77, background_firing=0)
+    pkw = dict(seed=77, background_firing=0, run_speed=dt)
     net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(**pkw, step_mode=MODES[mode]))
     o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw))
-    fxyz = np.asarray(xyz[[3, 120, 250, 399]], dtype=np.float32)
-    radius = np.asarray([0.5, 0.7, 0.4, 0.6], dtype=np.float32)
-    # 20 Hz is a whole number of 1 ms steps: it fires only once shifted (as the reference)
-    rates = np.asarray([20.0, 30.0, 47.3, 0.0], dtype=np.float32)
-    net.setInputRateArray(rates, inputPositions=fxyz, inputRadius=radius)
-    o.set_firers(rates, fxyz, radius)
-    net.record_raster(600)
-    rg = []
+    fxyz = np.asarray(xyz[[3, 120, 250, 399, 77]], dtype=np.float32)
+    radius = np.asarray([0.5, 0.7, 0.4, 0.6, 0.8], dtype=np.float32)
+    # at 1 ms, 20 Hz is a whole number of steps: it fires only once shifted (as the reference)
+    rates = np.asarray([20.0, 30.0, 47.3, 0.0], dtype=np.float32) * np.float32(scale)
+    net.setInputRateArray(rates, inputPositions=fxyz[:4], inputRadius=radius[:4])
+    o.set_firers(rates, fxyz[:4], radius[:4])
+    # offsets before the first step, seen by its time-0 run call
+    net.addInputOffset(1, 2.0 / scale)
+    o.add_firer_offset(1, 2.0 / scale)
+    net.record_raster(750)
     ro = []
-    for seg, action in enumerate(["none", "offset", "rates", "offset2"]):
+    for action in ["none", "offset", "rates", "append", "pop"]:
         if action == "offset":
             net.addInputOffset(0, 0.25)
             o.add_firer_offset(0, 0.25)
         elif action == "rates":
-            new = np.asarray([20.0, 12.5, 90.0, 33.0], dtype=np.float32)
-            net.set_input_rates(new)
-            o.set_firer_rates(new)
-        elif action == "offset2":
+            rates = np.asarray([20.0, 12.5, 90.0, 33.0], dtype=np.float32) * np.float32(scale)
+            net.set_input_rates(rates)
+            o.set_firer_rates(rates)
             net.addInputOffset(3, -0.75)
             o.add_firer_offset(3, -0.75)
+        elif action == "append":
+            rates = np.append(rates, np.float32(61.0 * scale))
+            net.setInputRateArray(rates, inputPositions=fxyz[4:], inputRadius=radius[4:])
+            o.set_firers(rates, fxyz, radius)
+        elif action == "pop":
+            rates = rates[[0, 1, 2]]
+            net.setInputRateArray(rates)
+            o.set_firers(rates, fxyz[:3], radius[:3])
         net.run(150)
         r, _ = o.run(150, raster=True)
         ro.append(r)

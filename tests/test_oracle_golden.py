@@ -94,6 +94,33 @@ def test_few_neurons_preset_known_answer(oracle_mod):
     assert w[250][0] == 1.0 and w[250][1] == 0.0
 
 
+def test_firer_schedule_matches_reference(oracle_mod):
+    """InputFirer::schedule (src/NeuCor.cpp:333-345) as the reference's own run calls
+    drive it: lastFire of every firer after each call, recorded from the reference at
+    steps that are (0.25, 1, 2 ms) and are not (0.02, 0.1, 0.3 ms) exact in float.  The
+    oracle's step t runs the call at time T_t (and step 1 also the one at time 0), so
+    after its step t it holds the reference's lastFire after call t."""
+    O = oracle_mod
+    fx = load("firer_schedule")
+    xyz = np.array([[0, 0, 0], [0.3, 0.3, 0], [0.3, -0.3, 0]], np.float32)
+    rates = fx["rates"]
+    nf = len(rates)
+    base = 0
+    for dt, steps in zip(fx["dts"], fx["steps"]):
+        rows = fx["last"][base: base + steps]
+        base += steps
+        o = O.OracleS(xyz, [0, 0], [1, 2], [0.5, 0.5], params=O.default_params(run_speed=float(dt), seed=1))
+        o.set_firers(rates, np.zeros((nf, 3), np.float32), np.full(nf, 0.1, np.float32))
+        for i, off in enumerate(fx["offsets"]):
+            o.add_firer_offset(i, float(off))
+        got = np.zeros((steps - 1, nf), np.float32)
+        for t in range(1, steps):
+            o.run(1)
+            got[t - 1] = o.firer_last()
+        np.testing.assert_array_equal(bits(got), bits(rows[1:]), err_msg=f"dt {dt}")
+        assert len(np.unique(rows[:, 3])) > 20  # the 700 Hz firer advanced
+
+
 def test_oracle_input_groups_rates(oracle_mod):
     """Poisson groups fire at their rate; correlated members share jittered events."""
     O = oracle_mod
