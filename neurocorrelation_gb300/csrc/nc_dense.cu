@@ -17,7 +17,8 @@
 //     ballot of "arrived in t-KC .. t-1" is one word of the window bitmap.
 //   k_dense_neurons (lane per neuron): charge_insynapses in ascending source order
 //     from the window bitmap, charge_passive, threshold, AP, background draws (as the
-//     event form's k_neuron_step).
+//     event form's k_neuron_step); the folds of the neurons outside their AP are
+//     compacted onto full warps.
 //
 // Launches of the fires of prev happen at the start of step t instead of the end of
 // step prev; nothing between those points reads what they write (a spike launched at
@@ -59,11 +60,11 @@ __device__ __forceinline__ int warp_sum(int v)
 
 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT) for the queued launches [0, count)
 // (src/NeuCor.cpp:695); lane l takes entry l.
-__device__ __forceinline__ void drain_terms(double* term_span, double e_term, SynShared& sh, int wib, int lane,
+__device__ __forceinline__ void drain_terms(NcTerm* term_span, double e_term, SynShared& sh, int wib, int lane,
                                             int count)
 {
     __syncwarp();
-    if (lane < count) term_span[sh.qs[wib][lane]] = __dmul_rn(__dmul_rn((double)sh.qx[wib][lane], 0.9943), e_term);
+    if (lane < count) term_span[sh.qs[wib][lane]] = make_term(sh.qx[wib][lane], e_term);
     __syncwarp();
 }
 
@@ -88,7 +89,7 @@ __device__ __forceinline__ void span_chunks(const NcPools& P, const NcNetDesc& D
     int32_t* ta_p = P.t_arr + s_span + lane;
     const uint32_t* inh_p = P.inh + (s_span >> 5);
     uint32_t* win_p = P.win + (s_span >> 5);
-    double* term_span = P.term + s_span;
+    NcTerm* term_span = P.term + s_span;
     const float dt = D.dt, c52 = D.c52;
     for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
         int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
@@ -466,7 +467,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
                         qn += __popc(lm);
                         if (qn >= 32) {
                             __syncwarp();
-                            P.term[ws.qs[lane]] = __dmul_rn(__dmul_rn((double)ws.qx[lane], 0.9943), D.e_term);
+                            P.term[ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
                             __syncwarp();
                             if (lane < qn - 32) {
                                 ws.qs[lane] = ws.qs[32 + lane];
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
                 }
             }
             __syncwarp();
-            if (lane < qn) P.term[ws.qs[lane]] = __dmul_rn(__dmul_rn((double)ws.qx[lane], 0.9943), D.e_term);
+            if (lane < qn) P.term[ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
             acc[0] += (unsigned long long)warp_sum(nl);
             acc[1] += (unsigned long long)warp_sum(nd);
         }
@@ -498,125 +499,174 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
     block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
 }
 
+// charge_insynapses (src/NeuCor.cpp:688-700) of neuron j of net D: the terms of the
+// spikes that arrived t-1 .. t-KC, in ascending source id, folded into pot.  The row's
+// window bits are read 256 synapses (8 words) at a time and streamed in batches of 8
+// across word boundaries, so that a warp's batch count is its busiest lane's, not a sum
+// of per-word maxima.
+__device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, int32_t j, float pot)
+{
+    const int64_t s0 = P.in_ptr[D.ptr_base + j];
+    const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
+    const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
+    for (int64_t wb = wa0; wb <= wa1; wb += 8) {
+        unsigned long long m[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int64_t wq = wb + 2 * q;
+            uint32_t x = wq <= wa1 ? P.win[wq] : 0u;
+            uint32_t y = wq + 1 <= wa1 ? P.win[wq + 1] : 0u;
+            if (wq == wa0) x &= ~0u << (s0 & 31);
+            if (wq == wa1 && (s1 & 31)) x &= (1u << (s1 & 31)) - 1u;
+            if (wq + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
+            m[q] = x | ((unsigned long long)y << 32);
+        }
+        const NcTerm* tp = P.term + wb * 32;
+        unsigned long long m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
+        int base = 0;
+        while (m0 | m1 | m2 | m3) {
+            int b[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                // on to the next pair when this one is spent (an empty pair costs a slot)
+                if (m0 == 0ull) {
+                    m0 = m1;
+                    m1 = m2;
+                    m2 = m3;
+                    m3 = 0ull;
+                    base += 64;
+                }
+                b[k] = m0 ? base + __ffsll((long long)m0) - 1 : -1;
+                m0 &= m0 - 1ull;
+            }
+            NcTerm v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (b[k] >= 0) v[k] = tp[b[k]];
+            pot = fold8(pot, v, b, tp, D.e_term);
+        }
+    }
+    return pot;
+}
+
+// Lane per neuron for the update, with the folds compacted: a warp takes kFoldTiles
+// tiles (of up to 32 neurons each), folds the neurons that need it 32 at a time, then
+// finishes every neuron of its tiles.  Inside its AP (t - lastFire < KC) a neuron's
+// potential comes from the AP table whatever its sum is, and it cannot cross the
+// threshold, so its fold is skipped; at saturation that is most of them.
+#ifndef NC_FOLD_TILES
+#define NC_FOLD_TILES 1
+#endif
+constexpr int kFoldTiles = NC_FOLD_TILES;
+
 __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcPools P)
 {
     __shared__ int s_net[kMaxWarps];
     __shared__ unsigned long long s_acc[kMaxWarps][1];
     __shared__ int s_last;
+    __shared__ float s_pot[kMaxWarps][kFoldTiles * 32];
+    __shared__ uint8_t s_list[kMaxWarps][kFoldTiles * 32];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
     const int nw = gridDim.x * (blockDim.x >> 5);
     const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
+    const uint32_t below = (1u << lane) - 1u;
 
     int acc_net = -1;
     unsigned long long acc[1] = {0};  // fires
-    for (int tix = gw; tix < n_tiles; tix += nw) {
-        const NcTile tile = P.tiles[tix];
-        const NcNetDesc& D = P.nets[tile.net];
-        const int32_t t = D.t;
-        if (!(D.active && t <= D.t_end)) continue;
-        if (tile.net != acc_net) {
-            if (acc_net >= 0 && lane == 0) atomicAdd(P.nets[acc_net].stats + 0, acc[0]);
-            acc_net = tile.net;
-            acc[0] = 0;
-        }
-        const int32_t first = tile.first;
-        const int32_t j = first + lane;
-        const bool live = j < D.n;
-        const int32_t pj = D.neuron_base + j;
-        const int64_t word = D.word_base + (first >> 5);
-        const int32_t kc = D.kc;
-        bool fired = false;
-        if (live) {
-            int32_t lf = P.lf[pj];
-            const int64_t s0 = P.in_ptr[D.ptr_base + j];
-            const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
-            float pot = P.pot[pj];
-            const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
-            const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
-            bool forced = (fw >> lane) & 1u;
-            if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
-            // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
-            // t-1 .. t-KC, ascending source id; the accumulator stays a float value
-            if (s1 > s0) {
-                double pd = (double)pot;
-                const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
-                // the row's window bits, 256 synapses (8 words) at a time, streamed in
-                // batches of 8 across word boundaries so that a warp's batch count is
-                // its busiest lane's, not a sum of per-word maxima
-                for (int64_t wb = wa0; wb <= wa1; wb += 8) {
-                    unsigned long long m[4];
+    for (int g0 = gw * kFoldTiles; g0 < n_tiles; g0 += nw * kFoldTiles) {
+        // the neurons of the warp's tiles that need their fold
+        uint32_t need_m[kFoldTiles];
+        int count = 0;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int64_t wq = wb + 2 * q;
-                        uint32_t x = wq <= wa1 ? P.win[wq] : 0u;
-                        uint32_t y = wq + 1 <= wa1 ? P.win[wq + 1] : 0u;
-                        if (wq == wa0) x &= ~0u << (s0 & 31);
-                        if (wq == wa1 && (s1 & 31)) x &= (1u << (s1 & 31)) - 1u;
-                        if (wq + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
-                        m[q] = x | ((unsigned long long)y << 32);
-                    }
-                    const double* tp = P.term + wb * 32;
-                    unsigned long long m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
-                    int base = 0;
-                    while (m0 | m1 | m2 | m3) {
-                        int b[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            // on to the next pair when this one is spent (an empty pair costs a slot)
-                            if (m0 == 0ull) {
-                                m0 = m1;
-                                m1 = m2;
-                                m2 = m3;
-                                m3 = 0ull;
-                                base += 64;
-                            }
-                            b[k] = m0 ? base + __ffsll((long long)m0) - 1 : -1;
-                            m0 &= m0 - 1ull;
-                        }
-                        double v[8];
-#pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            if (b[k] >= 0) v[k] = tp[b[k]];
-                        pd = fold8(pd, v, b, tp);
-                    }
+        for (int g = 0; g < kFoldTiles; ++g) {
+            bool need = false;
+            if (g0 + g < n_tiles) {
+                const NcTile tile = P.tiles[g0 + g];
+                const NcNetDesc& D = P.nets[tile.net];
+                const int32_t t = D.t;
+                const int32_t j = tile.first + lane;
+                if (D.active && t <= D.t_end && j < D.n) {
+                    const int32_t lf = P.lf[D.neuron_base + j];
+                    need = !(lf != NC_NEVER && t - lf < D.kc) &&
+                           P.in_ptr[D.ptr_base + j + 1] > P.in_ptr[D.ptr_base + j];
                 }
-                pot = __double2float_rn(pd);
             }
-            // charge_passive (src/NeuCor.cpp:677-680)
-            pot = (pot - -70.0f) * D.leak + -70.0f;
-            // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
-            const bool can = (lf == NC_NEVER) || (t - lf >= kc);
-            // an input firer's Neuron::fire has no threshold or refractory test
-            fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
-            if (fired) {
-                lf = t;
-                P.lf[pj] = t;
-                P.firings[pj] += 1u;
+            need_m[g] = __ballot_sync(kFull, need);
+            if (need) s_list[wib][count + __popc(need_m[g] & below)] = (uint8_t)(g * 32 + lane);
+            count += __popc(need_m[g]);
+        }
+        __syncwarp();
+        for (int r = lane; r < count; r += 32) {
+            const int ent = s_list[wib][r];
+            const NcTile tile = P.tiles[g0 + (ent >> 5)];
+            const NcNetDesc& D = P.nets[tile.net];
+            const int32_t j = tile.first + (ent & 31);
+            s_pot[wib][ent] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int g = 0; g < kFoldTiles; ++g) {
+            const int tix = g0 + g;
+            if (tix >= n_tiles) break;
+            const NcTile tile = P.tiles[tix];
+            const NcNetDesc& D = P.nets[tile.net];
+            const int32_t t = D.t;
+            if (!(D.active && t <= D.t_end)) continue;
+            if (tile.net != acc_net) {
+                if (acc_net >= 0 && lane == 0) atomicAdd(P.nets[acc_net].stats + 0, acc[0]);
+                acc_net = tile.net;
+                acc[0] = 0;
             }
-            // AP (src/NeuCor.cpp:706-714)
-            if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
-            P.pot[pj] = pot;
-        }
-        const uint32_t fmask = __ballot_sync(kFull, fired);
-        if (lane == 0) {
-            P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
-            P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
-            P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
-            if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
-                D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
-        }
-        acc[0] += (unsigned long long)__popc(fmask);
-        // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
-        if (live && D.bg_period > 0) {
-            uint32_t o[4];
-            philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
-            if (o[0] % (uint32_t)D.bg_period == 0u) {
-                uint32_t tgt = o[1] % (uint32_t)D.n;
-                if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
-                atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
-                         1u << (tgt & 31));
+            const int32_t first = tile.first;
+            const int32_t j = first + lane;
+            const bool live = j < D.n;
+            const int32_t pj = D.neuron_base + j;
+            const int64_t word = D.word_base + (first >> 5);
+            const int32_t kc = D.kc;
+            bool fired = false;
+            if (live) {
+                int32_t lf = P.lf[pj];
+                float pot = ((need_m[g] >> lane) & 1u) ? s_pot[wib][g * 32 + lane] : P.pot[pj];
+                const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
+                const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
+                bool forced = (fw >> lane) & 1u;
+                if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
+                // charge_passive (src/NeuCor.cpp:677-680)
+                pot = (pot - -70.0f) * D.leak + -70.0f;
+                // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
+                const bool can = (lf == NC_NEVER) || (t - lf >= kc);
+                // an input firer's Neuron::fire has no threshold or refractory test
+                fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
+                if (fired) {
+                    lf = t;
+                    P.lf[pj] = t;
+                    P.firings[pj] += 1u;
+                }
+                // AP (src/NeuCor.cpp:706-714)
+                if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
+                P.pot[pj] = pot;
+            }
+            const uint32_t fmask = __ballot_sync(kFull, fired);
+            if (lane == 0) {
+                P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
+                P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
+                P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
+                if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
+                    D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
+            }
+            acc[0] += (unsigned long long)__popc(fmask);
+            // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
+            if (live && D.bg_period > 0) {
+                uint32_t o[4];
+                philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
+                if (o[0] % (uint32_t)D.bg_period == 0u) {
+                    uint32_t tgt = o[1] % (uint32_t)D.n;
+                    if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
+                    atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
+                             1u << (tgt & 31));
+                }
             }
         }
     }
@@ -693,8 +743,8 @@ int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream)
 
 int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    const int wpb = L.neuron_block / 32;
-    const int blocks = (P.n_tiles + wpb - 1) / wpb;
+    const int per_block = L.neuron_block / 32 * kFoldTiles;  // tiles
+    const int blocks = (P.n_tiles + per_block - 1) / per_block;
     if (blocks > 0) k_dense_neurons<<<blocks, L.neuron_block, 0, (cudaStream_t)stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

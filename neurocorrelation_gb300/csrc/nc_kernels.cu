@@ -168,16 +168,18 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                 bool forced = (fw >> lane) & 1u;
                 if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
                 // charge_insynapses (src/NeuCor.cpp:688-700): terms of spikes that arrived
-                // t-1 .. t-KC, ascending source id; the accumulator stays a float value.
-                // The arrival branch of the deferred plasticity rides along: the spikes
-                // that arrived at prev are the ring bits of slot prev.
+                // t-1 .. t-KC, ascending source id.  The arrival branch of the deferred
+                // plasticity rides along: the spikes that arrived at prev are the ring
+                // bits of slot prev.  Inside its AP (t - lastFire < KC) a neuron's
+                // potential comes from the AP table whatever the sum is, and it cannot
+                // cross the threshold, so only its sum is skipped.
+                const bool in_ap = lf != NC_NEVER && t - lf < D.kc;
                 if (r1 > r0) {
                     uint32_t* ring = P.ring + D.ring_base;
                     const int64_t rw = D.ring_words;
                     const int32_t kc = D.kc;
                     const int32_t oldest = t - kc;
                     const float trT = trace_at(P.tables + D.table_base + D.tab_pre_len, D.tab_post_len, prev, lf);
-                    double pd = (double)pot;
                     for (int32_t wi = r0; wi < r1; wi += 2) {
                         const bool two = wi + 1 < r1;
                         uint32_t lo = 0, hi = 0, alo = 0, ahi = 0, olo = 0, ohi = 0;
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             olo = x;  // ends as the word of slot t-KC when t-KC >= 1
                             ohi = y;
                         }
-                        unsigned long long bits = lo | ((unsigned long long)hi << 32);
+                        unsigned long long bits = in_ap ? 0ull : (lo | ((unsigned long long)hi << 32));
                         const unsigned long long arr = stdp ? (alo | ((unsigned long long)ahi << 32)) : 0ull;
                         const int64_t sb = s0 + (int64_t)(wi - r0) * 32;
                         unsigned long long ih = 0ull;
@@ -218,12 +220,12 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                         while (bits) {
                             int b[8];
                             pop8_64(&bits, b);
-                            double v[8];
-                            const double* tp = P.term + sb;
+                            NcTerm v[8];
+                            const NcTerm* tp = P.term + sb;
 #pragma unroll
                             for (int k = 0; k < 8; ++k)
                                 if (b[k] >= 0) v[k] = tp[b[k]];
-                            pd = fold8(pd, v, b, tp);
+                            pot = fold8(pot, v, b, tp, D.e_term);
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
                         if (oldest >= 1) {
@@ -232,7 +234,6 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             if (two && ohi) orow[1] = 0u;
                         }
                     }
-                    pot = __double2float_rn(pd);
                 }
                 // charge_passive (src/NeuCor.cpp:677-680)
                 pot = (pot - -70.0f) * D.leak + -70.0f;
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPo
                 // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
                 const float depol = D.c52 * w;
                 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT)  (src/NeuCor.cpp:695)
-                P.term[s] = __dmul_rn(__dmul_rn((double)(D.dt * depol), 0.9943), D.e_term);
+                P.term[s] = make_term(D.dt * depol, D.e_term);
                 const int32_t d = (int32_t)(dl[u] & 0x3fffu);
                 P.last_arr[k] = t + d;
                 const uint32_t pos = P.out_ringpos[k];
