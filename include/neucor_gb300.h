@@ -298,7 +298,8 @@ typedef struct {
     int32_t launch_blocks;       /* event form: blocks of the spike launch */
     int32_t launch_block;        /* event form: threads per block of the spike launch (32..256) */
     int32_t graph_steps;         /* steps per captured CUDA graph */
-    int32_t dense_blocks;        /* dense form: blocks of the step launch; 0 = one warp per 32 neurons */
+    int32_t dense_blocks;        /* dense form: blocks of the synapse pass (a grid-stride loop over
+                                    256-synapse spans); 0 = 4 per SM */
 } nc_launch_config;
 
 int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out);

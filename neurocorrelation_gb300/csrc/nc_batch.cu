@@ -186,7 +186,7 @@ int nc_batch_autotune(nc_batch* b, int32_t steps_per_trial, nc_launch_config* be
                                   b->eng.graph_ticks, b->eng.L.dense_blocks};
     if (b->eng.dense) {
         for (int nb : {64, 128, 256})
-            for (int dbm : {0, 2, 4, 8})
+            for (int dbm : {0, 2, 3, 8})
                 for (int g : {16, 64})
                     cands.push_back(nc_launch_config{nb, cur.launch_blocks, cur.launch_block, g, sms * dbm});
     } else {

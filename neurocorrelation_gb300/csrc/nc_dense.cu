@@ -17,8 +17,7 @@
 //     ballot of "arrived in t-KC .. t-1" is one word of the window bitmap.
 //   k_dense_neurons (lane per neuron): charge_insynapses in ascending source order
 //     from the window bitmap, charge_passive, threshold, AP, background draws (as the
-//     event form's k_neuron_step); the folds of the neurons outside their AP are
-//     compacted onto full warps.
+//     event form's k_neuron_step); a neuron inside its AP skips its fold.
 //
 // Launches of the fires of prev happen at the start of step t instead of the end of
 // step prev; nothing between those points reads what they write (a spike launched at
@@ -60,7 +59,7 @@ __device__ __forceinline__ int warp_sum(int v)
 
 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT) for the queued launches [0, count)
 // (src/NeuCor.cpp:695); lane l takes entry l.
-__device__ __forceinline__ void drain_terms(NcTerm* term_span, double e_term, SynShared& sh, int wib, int lane,
+__device__ __forceinline__ void drain_terms(double* term_span, double e_term, SynShared& sh, int wib, int lane,
                                             int count)
 {
     __syncwarp();
@@ -89,7 +88,7 @@ __device__ __forceinline__ void span_chunks(const NcPools& P, const NcNetDesc& D
     int32_t* ta_p = P.t_arr + s_span + lane;
     const uint32_t* inh_p = P.inh + (s_span >> 5);
     uint32_t* win_p = P.win + (s_span >> 5);
-    NcTerm* term_span = P.term + s_span;
+    double* term_span = P.term + s_span;
     const float dt = D.dt, c52 = D.c52;
     for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
         int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
@@ -508,6 +507,8 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
 {
     const int64_t s0 = P.in_ptr[D.ptr_base + j];
     const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
+    if (s1 <= s0) return pot;
+    double pd = (double)pot;
     const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
     for (int64_t wb = wa0; wb <= wa1; wb += 8) {
         unsigned long long m[4];
@@ -521,7 +522,7 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
             if (wq + 1 == wa1 && (s1 & 31)) y &= (1u << (s1 & 31)) - 1u;
             m[q] = x | ((unsigned long long)y << 32);
         }
-        const NcTerm* tp = P.term + wb * 32;
+        const double* tp = P.term + wb * 32;
         unsigned long long m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
         int base = 0;
         while (m0 | m1 | m2 | m3) {
@@ -539,134 +540,90 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
                 b[k] = m0 ? base + __ffsll((long long)m0) - 1 : -1;
                 m0 &= m0 - 1ull;
             }
-            NcTerm v[8];
+            double v[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k)
                 if (b[k] >= 0) v[k] = tp[b[k]];
-            pot = fold8(pot, v, b, tp, D.e_term);
+            pd = fold8(pd, v, b, tp);
         }
     }
-    return pot;
+    return __double2float_rn(pd);
 }
 
-// Lane per neuron for the update, with the folds compacted: a warp takes kFoldTiles
-// tiles (of up to 32 neurons each), folds the neurons that need it 32 at a time, then
-// finishes every neuron of its tiles.  Inside its AP (t - lastFire < KC) a neuron's
+// Lane per neuron (warp per tile of 32).  Inside its AP (t - lastFire < KC) a neuron's
 // potential comes from the AP table whatever its sum is, and it cannot cross the
-// threshold, so its fold is skipped; at saturation that is most of them.
-#ifndef NC_FOLD_TILES
-#define NC_FOLD_TILES 1
-#endif
-constexpr int kFoldTiles = NC_FOLD_TILES;
-
+// threshold, so its fold is skipped.
 __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcPools P)
 {
     __shared__ int s_net[kMaxWarps];
     __shared__ unsigned long long s_acc[kMaxWarps][1];
     __shared__ int s_last;
-    __shared__ float s_pot[kMaxWarps][kFoldTiles * 32];
-    __shared__ uint8_t s_list[kMaxWarps][kFoldTiles * 32];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
     const int nw = gridDim.x * (blockDim.x >> 5);
     const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
-    const uint32_t below = (1u << lane) - 1u;
 
     int acc_net = -1;
     unsigned long long acc[1] = {0};  // fires
-    for (int g0 = gw * kFoldTiles; g0 < n_tiles; g0 += nw * kFoldTiles) {
-        // the neurons of the warp's tiles that need their fold
-        uint32_t need_m[kFoldTiles];
-        int count = 0;
-#pragma unroll
-        for (int g = 0; g < kFoldTiles; ++g) {
-            bool need = false;
-            if (g0 + g < n_tiles) {
-                const NcTile tile = P.tiles[g0 + g];
-                const NcNetDesc& D = P.nets[tile.net];
-                const int32_t t = D.t;
-                const int32_t j = tile.first + lane;
-                if (D.active && t <= D.t_end && j < D.n) {
-                    const int32_t lf = P.lf[D.neuron_base + j];
-                    need = !(lf != NC_NEVER && t - lf < D.kc) &&
-                           P.in_ptr[D.ptr_base + j + 1] > P.in_ptr[D.ptr_base + j];
-                }
-            }
-            need_m[g] = __ballot_sync(kFull, need);
-            if (need) s_list[wib][count + __popc(need_m[g] & below)] = (uint8_t)(g * 32 + lane);
-            count += __popc(need_m[g]);
+    for (int tix = gw; tix < n_tiles; tix += nw) {
+        const NcTile tile = P.tiles[tix];
+        const NcNetDesc& D = P.nets[tile.net];
+        const int32_t t = D.t;
+        if (!(D.active && t <= D.t_end)) continue;
+        if (tile.net != acc_net) {
+            if (acc_net >= 0 && lane == 0) atomicAdd(P.nets[acc_net].stats + 0, acc[0]);
+            acc_net = tile.net;
+            acc[0] = 0;
         }
-        __syncwarp();
-        for (int r = lane; r < count; r += 32) {
-            const int ent = s_list[wib][r];
-            const NcTile tile = P.tiles[g0 + (ent >> 5)];
-            const NcNetDesc& D = P.nets[tile.net];
-            const int32_t j = tile.first + (ent & 31);
-            s_pot[wib][ent] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
+        const int32_t first = tile.first;
+        const int32_t j = first + lane;
+        const bool live = j < D.n;
+        const int32_t pj = D.neuron_base + j;
+        const int64_t word = D.word_base + (first >> 5);
+        const int32_t kc = D.kc;
+        bool fired = false;
+        if (live) {
+            int32_t lf = P.lf[pj];
+            float pot = P.pot[pj];
+            const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
+            const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
+            bool forced = (fw >> lane) & 1u;
+            if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
+            if (!(lf != NC_NEVER && t - lf < kc)) pot = fold_row(P, D, j, pot);
+            // charge_passive (src/NeuCor.cpp:677-680)
+            pot = (pot - -70.0f) * D.leak + -70.0f;
+            // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
+            const bool can = (lf == NC_NEVER) || (t - lf >= kc);
+            // an input firer's Neuron::fire has no threshold or refractory test
+            fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
+            if (fired) {
+                lf = t;
+                P.lf[pj] = t;
+                P.firings[pj] += 1u;
+            }
+            // AP (src/NeuCor.cpp:706-714)
+            if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
+            P.pot[pj] = pot;
         }
-        __syncwarp();
-#pragma unroll 1
-        for (int g = 0; g < kFoldTiles; ++g) {
-            const int tix = g0 + g;
-            if (tix >= n_tiles) break;
-            const NcTile tile = P.tiles[tix];
-            const NcNetDesc& D = P.nets[tile.net];
-            const int32_t t = D.t;
-            if (!(D.active && t <= D.t_end)) continue;
-            if (tile.net != acc_net) {
-                if (acc_net >= 0 && lane == 0) atomicAdd(P.nets[acc_net].stats + 0, acc[0]);
-                acc_net = tile.net;
-                acc[0] = 0;
-            }
-            const int32_t first = tile.first;
-            const int32_t j = first + lane;
-            const bool live = j < D.n;
-            const int32_t pj = D.neuron_base + j;
-            const int64_t word = D.word_base + (first >> 5);
-            const int32_t kc = D.kc;
-            bool fired = false;
-            if (live) {
-                int32_t lf = P.lf[pj];
-                float pot = ((need_m[g] >> lane) & 1u) ? s_pot[wib][g * 32 + lane] : P.pot[pj];
-                const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
-                const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
-                bool forced = (fw >> lane) & 1u;
-                if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
-                // charge_passive (src/NeuCor.cpp:677-680)
-                pot = (pot - -70.0f) * D.leak + -70.0f;
-                // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
-                const bool can = (lf == NC_NEVER) || (t - lf >= kc);
-                // an input firer's Neuron::fire has no threshold or refractory test
-                fired = ((uw >> lane) & 1u) || ((-55.0f < pot || forced) && can);
-                if (fired) {
-                    lf = t;
-                    P.lf[pj] = t;
-                    P.firings[pj] += 1u;
-                }
-                // AP (src/NeuCor.cpp:706-714)
-                if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
-                P.pot[pj] = pot;
-            }
-            const uint32_t fmask = __ballot_sync(kFull, fired);
-            if (lane == 0) {
-                P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
-                P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
-                P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
-                if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
-                    D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
-            }
-            acc[0] += (unsigned long long)__popc(fmask);
-            // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
-            if (live && D.bg_period > 0) {
-                uint32_t o[4];
-                philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
-                if (o[0] % (uint32_t)D.bg_period == 0u) {
-                    uint32_t tgt = o[1] % (uint32_t)D.n;
-                    if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
-                    atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
-                             1u << (tgt & 31));
-                }
+        const uint32_t fmask = __ballot_sync(kFull, fired);
+        if (lane == 0) {
+            P.fired[(int64_t)(t & 1) * P.total_words + word] = fmask;
+            P.forced[(int64_t)(t & 1) * P.total_words + word] = 0u;
+            P.ufire[(int64_t)(t & 1) * P.total_words + word] = 0u;
+            if (D.raster_len > 0 && t >= D.raster_t0 && t - D.raster_t0 < D.raster_len)
+                D.raster[(int64_t)(t - D.raster_t0) * D.n_words + (first >> 5)] = fmask;
+        }
+        acc[0] += (unsigned long long)__popc(fmask);
+        // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
+        if (live && D.bg_period > 0) {
+            uint32_t o[4];
+            philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
+            if (o[0] % (uint32_t)D.bg_period == 0u) {
+                uint32_t tgt = o[1] % (uint32_t)D.n;
+                if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
+                atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (tgt >> 5),
+                         1u << (tgt & 31));
             }
         }
     }
@@ -704,10 +661,28 @@ __global__ void k_dense_mark_flushed(NcPools P)
 #define NC_DENSE_STAGED 0
 #endif
 
+// The synapse pass's grid: the launch configuration's, else a persistent grid of
+// kSynBlocksPerSM blocks per SM (one wave; each warp strides over many spans, and the
+// staged form keeps its next span's copies in flight meanwhile).  A grid of one span
+// per warp measured 12% (register form) to 25% (staged form) slower.
+constexpr int kSynBlocksPerSM = 4;
+
+int sm_count()
+{
+    static int sms[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (sms[dev] == 0 && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms[dev] = 152;
+    return sms[dev];
+}
+
 int syn_blocks(const NcPools& P, const nc::LaunchShape& L)
 {
     const int wpb = NC_DENSE_STAGED ? kStageWarps : kMaxWarps;
-    return L.dense_blocks > 0 ? L.dense_blocks : (P.n_spans + wpb - 1) / wpb;
+    const int full = (P.n_spans + wpb - 1) / wpb;
+    if (L.dense_blocks > 0) return L.dense_blocks;
+    return full < sm_count() * kSynBlocksPerSM ? full : sm_count() * kSynBlocksPerSM;
 }
 
 template <bool kFlush>
@@ -743,8 +718,8 @@ int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream)
 
 int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    const int per_block = L.neuron_block / 32 * kFoldTiles;  // tiles
-    const int blocks = (P.n_tiles + per_block - 1) / per_block;
+    const int wpb = L.neuron_block / 32;
+    const int blocks = (P.n_tiles + wpb - 1) / wpb;
     if (blocks > 0) k_dense_neurons<<<blocks, L.neuron_block, 0, (cudaStream_t)stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

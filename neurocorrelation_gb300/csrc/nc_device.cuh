@@ -1,6 +1,6 @@
 // nc_device.cuh — device helpers shared by the step kernels: the reference's
-// plasticity and trace arithmetic, the ordered `float += double` fold (nc_fold.h), the
-// input draws and bit iteration.
+// plasticity and trace arithmetic, the ordered `float += double` fold, the input draws
+// and bit iteration.
 #pragma once
 #include "nc_engine.cuh"
 
@@ -58,46 +58,11 @@ static __device__ __forceinline__ float plasticity(float w, bool inh, float trac
 
 // The charge_insynapses term of a launch, deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT)
 // (src/NeuCor.cpp:695) for x = deltaT*AP_depolFac.
-static __device__ __forceinline__ NcTerm make_term(float x, double e_term)
+static __device__ __forceinline__ double make_term(float x, double e_term)
 {
-    const double T = __dmul_rn(__dmul_rn((double)x, 0.9943), e_term);
-#if NC_FOLD_SPLIT
-    return nc_split_term(T, x);
-#else
-    return NcTerm{T};
-#endif
+    return __dmul_rn(__dmul_rn((double)x, 0.9943), e_term);
 }
 
-#if NC_FOLD_SPLIT
-// The batch's adds with the hardware double arithmetic on the exact terms.  Kept out of
-// line so that the rare redo below is a branch and not issued with every batch.
-static __device__ __noinline__ float fold_exact8(float p, const NcTerm* tp, double e_term, int b0, int b1, int b2,
-                                                 int b3, int b4, int b5, int b6, int b7)
-{
-    const int b[8] = {b0, b1, b2, b3, b4, b5, b6, b7};
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (b[k] >= 0) p = __double2float_rn(__dadd_rn((double)p, nc_term_value(tp[b[k]], e_term)));
-    return p;
-}
-
-// Folds v[k] = tp[b[k]] for every k with b[k] >= 0 (ascending) into the accumulator p:
-// `potential += term` with the reference's float/double rounding, on float arithmetic
-// (nc_add_term); a batch with a rare add is redone exactly.
-static __device__ __forceinline__ float fold8(float p, const NcTerm v[8], const int b[8], const NcTerm* tp,
-                                              double e_term)
-{
-    const float p0 = p;
-    uint32_t xp = __float_as_uint(p) & NC_FEXP;
-    bool rare = false;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (b[k] >= 0) p = nc_add_term(p, xp, v[k], rare);
-    if (__builtin_expect(rare, 0))
-        p = fold_exact8(p0, tp, e_term, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7]);
-    return p;
-}
-#else
 // RN32 of a double, returned as the (exactly representable) double: the 52-bit
 // fraction is rounded to 23 bits, half to even, with integer operations, so the one
 // double add of `float += double` (src/NeuCor.cpp:695) stays the only FP64 instruction
@@ -117,30 +82,33 @@ static __device__ __forceinline__ double rn32_int(double d, bool& rare)
 // Exact `float += double` of the terms tp[b_k] (b_k >= 0, in k order) with the
 // hardware conversion.  Kept out of line so that the rare redo below is a branch and
 // its conversions are not issued with every batch.
-static __device__ __noinline__ double fold_exact8(double pd, const NcTerm* tp, int b0, int b1, int b2, int b3, int b4,
+static __device__ __noinline__ double fold_exact8(double pd, const double* tp, int b0, int b1, int b2, int b3, int b4,
                                                   int b5, int b6, int b7)
 {
     const int b[8] = {b0, b1, b2, b3, b4, b5, b6, b7};
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        if (b[k] >= 0) pd = (double)__double2float_rn(__dadd_rn(pd, tp[b[k]].v));
+        if (b[k] >= 0) pd = (double)__double2float_rn(__dadd_rn(pd, tp[b[k]]));
     return pd;
 }
 
-// Folds v[k] = tp[b[k]] for every k with b[k] >= 0 (ascending) into the accumulator p:
-// `potential += term`, one double add and an integer rounding to float per term.
-static __device__ __forceinline__ float fold8(float p, const NcTerm v[8], const int b[8], const NcTerm* tp, double)
+// Folds v[k] = tp[b[k]] for every k with b[k] >= 0 (ascending) into pd, the float
+// accumulator held as a double: `potential += term`, one double add and an integer
+// rounding to float per term.  (A fold on float arithmetic alone — the term split into
+// its float rounding and an integer tail, Fast2Sum and a tie test — is exact too, but
+// measured slower on this GPU: a warp's double add costs the issue of about 55 integer
+// instructions here, and the float path's fallback near a potential's zero crossing
+// costs more.)
+static __device__ __forceinline__ double fold8(double pd, const double v[8], const int b[8], const double* tp)
 {
-    const double pd0 = (double)p;
-    double pd = pd0;
+    const double pd0 = pd;
     bool rare = false;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        if (b[k] >= 0) pd = rn32_int(__dadd_rn(pd, v[k].v), rare);
+        if (b[k] >= 0) pd = rn32_int(__dadd_rn(pd, v[k]), rare);
     if (__builtin_expect(rare, 0)) pd = fold_exact8(pd0, tp, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7]);
-    return (float)pd;
+    return pd;
 }
-#endif
 
 static __device__ __forceinline__ void philox(uint32_t a, uint32_t b, uint32_t stream, uint32_t c, const NcNetDesc& D,
                                        uint32_t out[4])

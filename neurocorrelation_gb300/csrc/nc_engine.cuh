@@ -11,7 +11,7 @@
 //   in_ptr    CSC row starts (n+1): in-synapses of target j, ascending source id
 //             — the order of the reference's std::map inSynapses (src/NeuCor.h:212)
 //   w, t_arr, term          per in-synapse (CSC order): weight, last arrival step,
-//                           contribution term captured at launch
+//                           contribution term captured at launch (double)
 //   inh                     one bit per in-synapse: Synapse::inhibitory
 //   out_ptr   CSR row starts (n+1) and per out-synapse (CSR order): target,
 //             CSC index, delay (bits 0-13; bit 14/15: the target's caller id is
@@ -25,21 +25,6 @@
 #pragma once
 #include <cstdint>
 #include <vector_types.h>
-
-#include "nc_fold.h"
-
-// Storage of the charge_insynapses terms: split for the FP64-free fold (nc_fold.h), or
-// the double itself for the hardware double add.
-#ifndef NC_FOLD_SPLIT
-#define NC_FOLD_SPLIT 0
-#endif
-#if NC_FOLD_SPLIT
-using NcTerm = NcSplitTerm;
-#else
-struct NcTerm {
-    double v;
-};
-#endif
 
 #ifdef __CUDACC__
 #define NC_HD __host__ __device__
@@ -137,7 +122,7 @@ struct NcPools {
     float* w;
     uint32_t* inh;       // Synapse::inhibitory, one bit per synapse
     int32_t* t_arr;
-    NcTerm* term;        // last launch's charge_insynapses term
+    double* term;        // last launch's charge_insynapses term (src/NeuCor.cpp:695)
     // out-synapses (CSR)
     int32_t* out_post;   // local target id
     int32_t* out_csc;    // CSC index relative to syn_base

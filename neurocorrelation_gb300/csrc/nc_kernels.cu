@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                 // cross the threshold, so only its sum is skipped.
                 const bool in_ap = lf != NC_NEVER && t - lf < D.kc;
                 if (r1 > r0) {
+                    double pd = (double)pot;
                     uint32_t* ring = P.ring + D.ring_base;
                     const int64_t rw = D.ring_words;
                     const int32_t kc = D.kc;
@@ -220,12 +221,12 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                         while (bits) {
                             int b[8];
                             pop8_64(&bits, b);
-                            NcTerm v[8];
-                            const NcTerm* tp = P.term + sb;
+                            double v[8];
+                            const double* tp = P.term + sb;
 #pragma unroll
                             for (int k = 0; k < 8; ++k)
                                 if (b[k] >= 0) v[k] = tp[b[k]];
-                            pot = fold8(pot, v, b, tp, D.e_term);
+                            pd = fold8(pd, v, b, tp);
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
                         if (oldest >= 1) {
@@ -234,6 +235,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             if (two && ohi) orow[1] = 0u;
                         }
                     }
+                    pot = __double2float_rn(pd);
                 }
                 // charge_passive (src/NeuCor.cpp:677-680)
                 pot = (pot - -70.0f) * D.leak + -70.0f;

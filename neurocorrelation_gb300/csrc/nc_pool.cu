@@ -182,7 +182,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(P.w, float, syn);
     NC_ALLOC(P.inh, uint32_t, (syn + 31) / 32 + 1);  // one spare word for 32-bit windows
     NC_ALLOC(P.t_arr, int32_t, syn);
-    NC_ALLOC(P.term, NcTerm, syn);
+    NC_ALLOC(P.term, double, syn);
     if (dense) {
         NC_ALLOC(P.csc_pre, int32_t, syn);
         NC_ALLOC(P.csc_post, int32_t, syn);

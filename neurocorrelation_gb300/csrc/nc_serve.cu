@@ -229,7 +229,7 @@ int nc_server::init(std::string& err)
     S_AL(P.w, float, syn_cap);
     S_AL(P.inh, uint32_t, syn_cap / 32 + 1);
     S_AL(P.t_arr, int32_t, syn_cap);
-    S_AL(P.term, NcTerm, syn_cap);
+    S_AL(P.term, double, syn_cap);
     if (dense) {
         span_cap = syn_cap / (32 * NC_SPAN_CHUNKS) + nets;
         S_AL(P.csc_pre, int32_t, syn_cap);
