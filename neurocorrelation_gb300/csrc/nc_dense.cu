@@ -6,8 +6,10 @@
 // near one fire per refractory period), nearly every in-row is touched every step
 // anyway, and streaming the rows in order is cheaper than scattering into them.
 //
-//   k_dense_synapses (warp per span of 8 x 32 in-synapses, CSC order, coalesced), for
-//   the step prev = t-1 of the span's net:
+//   k_dense_synapses (warp per span of 8 x 32 in-synapses, CSC order; the span's
+//   streams arrive by bulk copies into shared memory, the next ones in flight while a
+//   warp works; k_dense_synapses_direct is the same pass on register loads), for the
+//   step prev = t-1 of the span's net:
 //     Synapse::fire of every in-synapse whose source fired at prev (src/NeuCor.cpp:
 //     727-738): dropped while busy, otherwise it captures fl(fl(0.2f*52)*w) and its
 //     arrival step; then the plasticity of prev (src/NeuCor.cpp:740-761): post-spike
@@ -68,7 +70,7 @@ __device__ __forceinline__ void drain_terms(double* term_span, double e_term, Sy
 }
 
 // Synapse::fire and the deferred plasticity of step `prev` for the span's chunks (see
-// k_dense_synapses); kAll: every chunk of the span lies inside the net.
+// k_dense_synapses_direct); kAll: every chunk of the span lies inside the net.
 template <bool kAll>
 __device__ __forceinline__ void span_chunks(const NcPools& P, const NcNetDesc& D, SynShared& sh, int wib, int lane,
                                             int64_t s_span, int32_t rem, int32_t t, int32_t prev, int& qn, int& nl,
@@ -213,7 +215,7 @@ __device__ void block_counters(const NcPools& P, int* s_net, unsigned long long 
 }
 
 template <bool kFlush>
-__global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses(NcPools P)
+__global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses_direct(NcPools P)
 {
     __shared__ SynShared sh;
     __shared__ int s_net[kMaxWarps];
@@ -260,27 +262,45 @@ __global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses(NcP
 }
 
 // ---------------------------------------------------------------- staged synapse pass
-// The same pass with the span's six in-synapse streams staged into shared memory by the
-// bulk-copy (TMA) engine: each warp keeps the next span's copies in flight while it
-// works on the current one, so the memory system sees ~11 KB per warp outstanding
-// instead of the few loads a warp's registers can hold.
+// The same pass with the six in-synapse streams staged into shared memory by the
+// bulk-copy (TMA) engine.  A warp works through its spans in units of half a span
+// (4 chunks, 128 synapses) and keeps the next unit's copies in flight while it works
+// on the current one (a ring of stage buffers, one mbarrier each): the memory system
+// sees the copies in flight whatever the warp's registers hold, and 24 warps per SM
+// (8 per block, 3 blocks) cover the compute's own latencies.  Shapes measured on the
+// 100k x 100 network (us per pass): 8 warps / half-span units / 2 stages 103,
+// 6 / whole spans / 2 stages 104, 4 / whole / 2 105, 6 / half / 3 110, 4 / half / 4
+// 119, 4 / whole / 3 136.
 
-constexpr int kStageWarps = 4;  // 128-thread blocks
-constexpr int kSpanSyn = NC_SPAN_CHUNKS * 32;
+#ifndef NC_STAGE_WARPS
+#define NC_STAGE_WARPS 8
+#endif
+#ifndef NC_STAGE_UNIT
+#define NC_STAGE_UNIT 4
+#endif
+#ifndef NC_STAGE_DEPTH
+#define NC_STAGE_DEPTH 2
+#endif
+constexpr int kStageWarps = NC_STAGE_WARPS;  // warps per block
+constexpr int kUnitChunks = NC_STAGE_UNIT;   // chunks per staged unit
+constexpr int kUnitSyn = kUnitChunks * 32;
+constexpr int kUnitsPerSpan = NC_SPAN_CHUNKS / kUnitChunks;
+constexpr int kStages = NC_STAGE_DEPTH;      // units in flight per warp, the current one included
+static_assert(NC_SPAN_CHUNKS % kUnitChunks == 0 && kUnitChunks % kUnroll == 0, "unit shape");
 
-struct StageBuf {                 // one span, as laid out in the pools (16-byte multiples)
-    int32_t pre[kSpanSyn];
-    int32_t post[kSpanSyn];
-    int32_t la[kSpanSyn];
-    float w[kSpanSyn];
-    int32_t ta[kSpanSyn];
-    uint16_t dl[kSpanSyn];
+struct StageBuf {                 // one unit, as laid out in the pools (16-byte multiples)
+    int32_t pre[kUnitSyn];
+    int32_t post[kUnitSyn];
+    int32_t la[kUnitSyn];
+    float w[kUnitSyn];
+    int32_t ta[kUnitSyn];
+    uint16_t dl[kUnitSyn];
 };
 
-struct WarpStage {
-    StageBuf buf[2];
-    unsigned long long bar[2];    // mbarriers: the copies of buf[k] have landed
-    int64_t qs[kQueue];
+struct __align__(16) WarpStage {
+    StageBuf buf[kStages];
+    unsigned long long bar[kStages];  // mbarriers: the copies of buf[k] have landed
+    int32_t qs[kQueue];               // launched synapse, relative to its span's first
     float qx[kQueue];
 };
 
@@ -298,17 +318,20 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
                  :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
-// Lane 0: copies span `sp` into b (all six streams), completing on *bar.  Returns 0
-// when the span's net is skipped this launch (nothing copied).
-__device__ int stage_span(const NcPools& P, int sp, bool flush, StageBuf* b, unsigned long long* bar)
+// Lane 0: copies unit `half` of span `sp` into b (all six streams), completing on *bar.
+// Returns 0 when nothing is copied: the span's net is skipped this launch, or the unit
+// lies past the net's last synapse.
+__device__ int stage_unit(const NcPools& P, int sp, int half, bool flush, StageBuf* b, unsigned long long* bar)
 {
     const NcTile span = P.spans[sp];
     const NcNetDesc& D = P.nets[span.net];
     const int32_t t = D.t, prev = t - 1;
     if (!D.active || prev < 1 || D.stdp_done >= prev || (!flush && t > D.t_end)) return 0;
     const int64_t chunks = (D.n_syn + 31) / 32;
-    const int64_t nch = min((int64_t)NC_SPAN_CHUNKS, chunks - span.first);
-    const int64_t s = D.syn_base + (int64_t)span.first * 32;
+    const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
+    const int64_t nch = min((int64_t)kUnitChunks, chunks - c0);
+    if (nch <= 0) return 0;
+    const int64_t s = D.syn_base + c0 * 32;
     const uint32_t b4 = (uint32_t)(nch * 128), b2 = (uint32_t)(nch * 64);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)), "r"(5 * b4 + b2)
                  : "memory");
@@ -335,7 +358,7 @@ __device__ __forceinline__ bool stage_wait(unsigned long long* bar, uint32_t pha
 }
 
 template <bool kFlush>
-__global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(NcPools P)
+__global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools P)
 {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
     __shared__ int s_net[kStageWarps];
@@ -348,33 +371,50 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
     WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[wib];
 
     if (lane == 0) {
-        for (int k = 0; k < 2; ++k)
+        for (int k = 0; k < kStages; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&ws.bar[k])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
 
+    // unit k of this warp: half k % kUnitsPerSpan of span gw + (k / kUnitsPerSpan) * nw,
+    // staged in slot k % kStages
+    int iss = 0;  // lane 0: bit j set = slot j holds an issued unit not yet consumed
+    if (lane == 0)
+        for (int k = 0; k < kStages - 1; ++k) {
+            const int sp = gw + (k / kUnitsPerSpan) * nw;
+            if (sp < n_spans && stage_unit(P, sp, k % kUnitsPerSpan, kFlush, &ws.buf[k], &ws.bar[k])) iss |= 1 << k;
+        }
+
     int acc_net = -1;
     unsigned long long acc[2] = {0, 0};  // launched, dropped
-    uint32_t phases = 0u;  // bit k: parity of buf[k]'s next completion
-    int cur = 0;
-    int issued = 0;  // lane 0's answer for the buffer `cur`, broadcast below
-    if (gw < n_spans && lane == 0) issued = stage_span(P, gw, kFlush, &ws.buf[0], &ws.bar[0]);
+    uint32_t phases = 0u;  // bit j: parity of slot j's next completion
     bool ok = true;
-    for (int sp = gw; sp < n_spans && ok; sp += nw) {
-        const int nxt = sp + nw;
-        int issued_next = 0;
-        if (nxt < n_spans && lane == 0) issued_next = stage_span(P, nxt, kFlush, &ws.buf[cur ^ 1], &ws.bar[cur ^ 1]);
-        const int this_issued = __shfl_sync(kFull, issued, 0);
-        issued = issued_next;
-        if (this_issued) {
-            if (!stage_wait(&ws.bar[cur], (phases >> cur) & 1u)) {
+    int qn = 0, nl = 0, nd = 0;
+    for (int k = 0;; ++k) {
+        const int sp = gw + (k / kUnitsPerSpan) * nw;
+        if (sp >= n_spans) break;
+        const int half = k % kUnitsPerSpan;
+        const int slot = k % kStages;
+        {
+            // the slot consumed last iteration takes unit k + kStages - 1
+            const int kn = k + kStages - 1, sn = kn % kStages;
+            const int spn = gw + (kn / kUnitsPerSpan) * nw;
+            if (lane == 0) {
+                iss &= ~(1 << sn);
+                if (spn < n_spans && stage_unit(P, spn, kn % kUnitsPerSpan, kFlush, &ws.buf[sn], &ws.bar[sn]))
+                    iss |= 1 << sn;
+            }
+        }
+        const int bits = __shfl_sync(kFull, iss, 0);
+        if ((bits >> slot) & 1) {
+            if (!stage_wait(&ws.bar[slot], (phases >> slot) & 1u)) {
                 if (lane == 0) atomicOr(P.dev_err, NC_DEV_ERR_STAGE_TIMEOUT);
                 ok = false;
                 break;
             }
-            phases ^= 1u << cur;
-            const StageBuf& B = ws.buf[cur];
+            phases ^= 1u << slot;
+            const StageBuf& B = ws.buf[slot];
             const NcTile span = P.spans[sp];
             const NcNetDesc& D = P.nets[span.net];
             const int32_t t = D.t;
@@ -390,19 +430,20 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
             }
             const int64_t sb = D.syn_base;
             const int64_t nsyn = D.n_syn;
+            const int64_t s_span = sb + (int64_t)span.first * 32;
             const int32_t kc = D.kc;
             const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
             const int32_t* lfn = P.lf + D.neuron_base;
             const float* tab_pre = P.tables + D.table_base;
             const float* tab_post = tab_pre + D.tab_pre_len;
-            int qn = 0, nl = 0, nd = 0;
-            for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
+            const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
+            for (int h = 0; h < kUnitChunks; h += kUnroll) {
                 uint32_t fword[kUnroll], ihw[kUnroll];
                 int32_t lfp[kUnroll];
                 bool in[kUnroll];
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u) {
-                    const int64_t c = span.first + h + u;
+                    const int64_t c = c0 + h + u;
                     const int q = (h + u) * 32 + lane;
                     in[u] = c * 32 + lane < nsyn;
                     fword[u] = 0u;
@@ -416,7 +457,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
                 }
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u) {
-                    const int64_t c = span.first + h + u;
+                    const int64_t c = c0 + h + u;
                     const int q = (h + u) * 32 + lane;
                     const int64_t s = sb + c * 32 + lane;
                     const int32_t la = B.la[q];
@@ -460,13 +501,13 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
                     if (lm) {
                         if (launch) {
                             const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                            ws.qs[pos] = s;
+                            ws.qs[pos] = (int32_t)(s - s_span);
                             ws.qx[pos] = x;
                         }
                         qn += __popc(lm);
                         if (qn >= 32) {
                             __syncwarp();
-                            P.term[ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                            P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
                             __syncwarp();
                             if (lane < qn - 32) {
                                 ws.qs[lane] = ws.qs[32 + lane];
@@ -478,22 +519,29 @@ __global__ void __launch_bounds__(32 * kStageWarps, 4) k_dense_synapses_staged(N
                     }
                 }
             }
-            __syncwarp();
-            if (lane < qn) P.term[ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
-            acc[0] += (unsigned long long)warp_sum(nl);
-            acc[1] += (unsigned long long)warp_sum(nd);
+            // the queue holds offsets into this span: drain it before the warp moves on
+            // to another span (the span's next unit follows when it was issued)
+            const bool more = half + 1 < kUnitsPerSpan && ((bits >> ((k + 1) % kStages)) & 1);
+            if (!more) {
+                __syncwarp();
+                if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                qn = 0;
+                acc[0] += (unsigned long long)warp_sum(nl);
+                acc[1] += (unsigned long long)warp_sum(nd);
+                nl = nd = 0;
+            }
         }
-        // the buffer is refilled by the next iteration's copy: finish reading it first,
-        // and order those reads before the copy engine's writes
+        // the slot is refilled next iteration: finish reading it first, and order those
+        // reads before the copy engine's writes
         __syncwarp();
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        cur ^= 1;
     }
     if (!ok) {
         // let this warp's copies in flight land (bounded) before the block's shared
-        // memory goes away: the one that timed out and the prefetch behind it
-        stage_wait(&ws.bar[cur], (phases >> cur) & 1u);
-        if (__shfl_sync(kFull, issued, 0)) stage_wait(&ws.bar[cur ^ 1], (phases >> (cur ^ 1)) & 1u);
+        // memory goes away: the one that timed out and the ones issued behind it
+        const int bits = __shfl_sync(kFull, iss, 0);
+        for (int j = 0; j < kStages; ++j)
+            if ((bits >> j) & 1) stage_wait(&ws.bar[j], (phases >> j) & 1u);
     }
     block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
 }
@@ -657,52 +705,59 @@ __global__ void k_dense_mark_flushed(NcPools P)
     }
 }
 
+// The staged synapse pass (bulk copies into shared memory) is the default; the
+// register-load form measured 5% slower on the persistent grid.
 #ifndef NC_DENSE_STAGED
-#define NC_DENSE_STAGED 0
+#define NC_DENSE_STAGED 1
 #endif
 
-// The synapse pass's grid: the launch configuration's, else a persistent grid of
-// kSynBlocksPerSM blocks per SM (one wave; each warp strides over many spans, and the
-// staged form keeps its next span's copies in flight meanwhile).  A grid of one span
-// per warp measured 12% (register form) to 25% (staged form) slower.
-constexpr int kSynBlocksPerSM = 4;
+// The synapse pass's grid: the launch configuration's, else a persistent grid of as
+// many blocks as fit on the GPU at once (one wave; each warp strides over many spans,
+// and the staged form keeps its next units' copies in flight meanwhile).  A grid of
+// one span per warp measured 12% (register form) to 25% (staged form) slower.
+struct SynKernel {
+    void (*fn)(NcPools);
+    int threads;
+    size_t smem;
+};
 
-int sm_count()
+template <bool kFlush>
+SynKernel syn_kernel()
 {
-    static int sms[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (sms[dev] == 0 && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        sms[dev] = 152;
-    return sms[dev];
+    if (NC_DENSE_STAGED) return {k_dense_synapses<kFlush>, 32 * kStageWarps, kStageSmem};
+    return {k_dense_synapses_direct<kFlush>, 32 * kMaxWarps, 0};
 }
 
-int syn_blocks(const NcPools& P, const nc::LaunchShape& L)
+// Blocks of the persistent grid on the current device (cached per device; the staged
+// form's shared-memory opt-in is set here, before the first launch).
+template <bool kFlush>
+int resident_blocks()
 {
-    const int wpb = NC_DENSE_STAGED ? kStageWarps : kMaxWarps;
-    const int full = (P.n_spans + wpb - 1) / wpb;
-    if (L.dense_blocks > 0) return L.dense_blocks;
-    return full < sm_count() * kSynBlocksPerSM ? full : sm_count() * kSynBlocksPerSM;
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (cache[dev] == 0) {
+        const SynKernel k = syn_kernel<kFlush>();
+        if (k.smem > 48 * 1024)
+            cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.threads, k.smem);
+        cache[dev] = sms * per_sm > 0 ? sms * per_sm : 1;
+    }
+    return cache[dev];
 }
 
 template <bool kFlush>
 int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
 {
-    const int blocks = syn_blocks(P, L);
+    const SynKernel k = syn_kernel<kFlush>();
+    const int wpb = k.threads / 32;
+    const int full = (P.n_spans + wpb - 1) / wpb;
+    const int resident = resident_blocks<kFlush>();
+    const int blocks = L.dense_blocks > 0 ? L.dense_blocks : (full < resident ? full : resident);
     if (blocks <= 0) return 0;
-    if (NC_DENSE_STAGED) {
-        static bool attr_set[64] = {};
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-            cudaFuncSetAttribute(k_dense_synapses_staged<kFlush>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kStageSmem);
-            attr_set[dev] = true;
-        }
-        k_dense_synapses_staged<kFlush><<<blocks, 32 * kStageWarps, kStageSmem, s>>>(P);
-    } else {
-        k_dense_synapses<kFlush><<<blocks, 32 * kMaxWarps, 0, s>>>(P);
-    }
+    k.fn<<<blocks, k.threads, k.smem, s>>>(P);
     return 0;
 }
 
@@ -722,6 +777,11 @@ int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
     const int blocks = (P.n_tiles + wpb - 1) / wpb;
     if (blocks > 0) k_dense_neurons<<<blocks, L.neuron_block, 0, (cudaStream_t)stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int prepare_dense_launch()
+{
+    return resident_blocks<false>() > 0 && resident_blocks<true>() > 0 ? 0 : -1;
 }
 
 int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream)

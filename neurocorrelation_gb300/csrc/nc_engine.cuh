@@ -226,6 +226,9 @@ int launch_stdp_flush(const NcPools& P, const LaunchShape& L, void* stream);
 // plasticity flush (the synapse pass of the last step's fires) before read-back.
 int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream);
+// Sizes the dense synapse pass's persistent grid (and sets its shared-memory opt-in) on
+// the current device; called before a stream capture, where neither may happen.
+int prepare_dense_launch();
 int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);

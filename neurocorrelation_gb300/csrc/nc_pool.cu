@@ -292,6 +292,7 @@ int Engine::capture_graph(std::string& err)
 {
     release_graph();
     cudaGraph_t g = nullptr;
+    if (dense) prepare_dense_launch();
     NC_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int k = 0; k < graph_ticks && rc == 0; ++k) rc |= launch_tick(stream);

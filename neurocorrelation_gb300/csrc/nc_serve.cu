@@ -293,6 +293,7 @@ int nc_server::capture(std::string& err)
     G.n_tiles = (int32_t)std::min<int64_t>(tile_cap, 1 << 30);
     nc::LaunchShape shape = L;
     cudaGraph_t g = nullptr;
+    if (dense) nc::prepare_dense_launch();
     S_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     const int nb_tiles = 152 * 16 * (shape.neuron_block / 32);  // grid of the captured neuron update
