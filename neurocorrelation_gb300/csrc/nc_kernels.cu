@@ -49,6 +49,8 @@ __device__ void postfire_rows(const NcPools& P, const NcNetDesc& D, int64_t word
                               int32_t prev)
 {
     const float* tab_pre = P.tables + D.table_base;
+    const int32_t tpl = D.tab_pre_len;
+    const Rates R = rates_of(D);
     uint32_t m = P.fired[(int64_t)(prev & 1) * P.total_words + word];
     while (m) {
         const int ba = __ffs(m) - 1;
@@ -78,7 +80,7 @@ __device__ void postfire_rows(const NcPools& P, const NcNetDesc& D, int64_t word
             for (int u = 0; u < 8; ++u) {
                 if (!ok[u]) continue;
                 const int64_t s = (u < 4 ? a0 : c0) + off + lane + 32 * (u & 3);
-                P.w[s] = plasticity(wv[u], ih[u], trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
+                P.w[s] = plasticity(wv[u], ih[u], trace_at(tab_pre, tpl, prev, ta[u]), 0.0f, R);
             }
         }
     }
@@ -94,6 +96,7 @@ __device__ void arrival_row(const NcPools& P, const NcNetDesc& D, int64_t s0, in
     const float* tab_post = P.tables + D.table_base + D.tab_pre_len;
     const uint32_t* slot = P.ring + D.ring_base + (int64_t)(prev & D.ring_mask) * D.ring_words;
     const float trT = trace_at(tab_post, D.tab_post_len, prev, lf);
+    const Rates R = rates_of(D);
     for (int32_t wi = r0; wi < r1; ++wi) {
         uint32_t bits = slot[wi];
         if (!bits) continue;
@@ -110,7 +113,7 @@ __device__ void arrival_row(const NcPools& P, const NcNetDesc& D, int64_t s0, in
             for (int k = 0; k < 8; ++k) {
                 if (b[k] < 0) continue;
                 P.t_arr[cs + b[k]] = prev;
-                P.w[cs + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1u, 0.0f, trT, D);
+                P.w[cs + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1u, 0.0f, trT, R);
             }
         }
     }
@@ -181,6 +184,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                     const int32_t kc = D.kc;
                     const int32_t oldest = t - kc;
                     const float trT = trace_at(P.tables + D.table_base + D.tab_pre_len, D.tab_post_len, prev, lf);
+                    const Rates R = rates_of(D);
                     for (int32_t wi = r0; wi < r1; wi += 2) {
                         const bool two = wi + 1 < r1;
                         uint32_t lo = 0, hi = 0, alo = 0, ahi = 0, olo = 0, ohi = 0;
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             for (int k = 0; k < 8; ++k) {
                                 if (b[k] < 0) continue;
                                 P.t_arr[sb + b[k]] = prev;
-                                P.w[sb + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1ull, 0.0f, trT, D);
+                                P.w[sb + b[k]] = plasticity(wv[k], (ih >> b[k]) & 1ull, 0.0f, trT, R);
                             }
                         }
                         while (bits) {
@@ -338,6 +342,13 @@ __global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPo
         const uint32_t* fired_t = P.fired + (int64_t)(t & 1) * P.total_words + D.word_base;
         const float* tab_pre = P.tables + D.table_base;
         uint32_t* ring = P.ring + D.ring_base;
+        // the descriptor's fields in registers: it lives in global memory, where every
+        // store below could alias it
+        const int32_t kc = D.kc, tpl = D.tab_pre_len, ring_mask = D.ring_mask;
+        const int64_t syn_base = D.syn_base, ring_words = D.ring_words;
+        const float dt = D.dt, c52 = D.c52;
+        const Rates R = rates_of(D);
+        const double e_term = D.e_term;
         int nl = 0, nd = 0;
         // four out-synapses per lane in flight: table loads, then weight loads, then writes
         for (int64_t kb = k0; kb < k1; kb += 128) {
@@ -359,8 +370,8 @@ __global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPo
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 // freed by the target's update at t only if the target's id is not above
-                acc[u] = ok[u] && (la[u] == NC_NEVER || t - la[u] >= D.kc + (int32_t)((dl[u] >> 14) & 1u));
-                if (acc[u]) wv[u] = P.w[D.syn_base + cs[u]];
+                acc[u] = ok[u] && (la[u] == NC_NEVER || t - la[u] >= kc + (int32_t)((dl[u] >> 14) & 1u));
+                if (acc[u]) wv[u] = P.w[syn_base + cs[u]];
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -370,21 +381,21 @@ __global__ void __launch_bounds__(256, NC_LAUNCH_MIN_BLOCKS) k_spike_launch(NcPo
                     continue;
                 }
                 const int64_t k = kb + lane + 32 * u;
-                const int64_t s = D.syn_base + cs[u];
+                const int64_t s = syn_base + cs[u];
                 float w = wv[u];
                 if ((dl[u] >> 15) & 1u) {  // target id below the source's: its update ran first
                     const int32_t j = P.out_post[k];
                     if ((fired_t[j >> 5] >> (j & 31)) & 1u)
-                        w = plasticity(w, inh_bit(P, s), trace_at(tab_pre, D.tab_pre_len, t, P.t_arr[s]), 0.0f, D);
+                        w = plasticity(w, inh_bit(P, s), trace_at(tab_pre, tpl, t, P.t_arr[s]), 0.0f, R);
                 }
                 // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                const float depol = D.c52 * w;
+                const float depol = c52 * w;
                 // deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT)  (src/NeuCor.cpp:695)
-                P.term[s] = make_term(D.dt * depol, D.e_term);
+                P.term[s] = make_term(dt * depol, e_term);
                 const int32_t d = (int32_t)(dl[u] & 0x3fffu);
                 P.last_arr[k] = t + d;
                 const uint32_t pos = P.out_ringpos[k];
-                atomicOr(ring + (int64_t)((t + d) & D.ring_mask) * D.ring_words + (pos >> 5), 1u << (pos & 31));
+                atomicOr(ring + (int64_t)((t + d) & ring_mask) * ring_words + (pos >> 5), 1u << (pos & 31));
                 ++nl;
             }
         }
