@@ -94,10 +94,12 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     int sms = 0;
     NC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    L.neuron_block = 256;
+    dense = nets.empty() || nets[0]->p.step_mode == NC_STEP_DENSE;
+    // the dense neuron pass is one wave: 128-thread blocks spread it more evenly over the
+    // SMs (measured 2% faster on the 100k x 100 network than 256)
+    L.neuron_block = dense ? 128 : 256;
     L.launch_block = 256;
     L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
-    dense = nets.empty() || nets[0]->p.step_mode == NC_STEP_DENSE;
 
     // pool sizes
     int64_t neurons = 0, ptrs = 0, words = 0, syn = 0, ring = 0, tables = 0, tiles = 0, spans = 0;

@@ -278,10 +278,10 @@ int nc_server::init(std::string& err)
     a_ring.reset(ring_cap);
     a_table.reset(table_cap);
     for (int32_t q = nets - 1; q >= 0; --q) free_slots.push_back(q);
-    L.neuron_block = 256;
+    L.neuron_block = dense ? 128 : 256;
     L.launch_block = 256;
     L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
-    L.dense_blocks = std::max(1, sms * NC_DENSE_MIN_BLOCKS);  // warps stride the tile table
+    L.dense_blocks = 0;  // the synapse pass's persistent grid (its warps stride the span table)
     S_CK(cudaStreamSynchronize(stream));
     return capture(err);
 }
@@ -291,6 +291,9 @@ int nc_server::capture(std::string& err)
     // the neuron update strides over the tile table, so its grid need not follow it
     NcPools G = P;
     G.n_tiles = (int32_t)std::min<int64_t>(tile_cap, 1 << 30);
+    // likewise the synapse pass strides over the span table (its kernels read the live
+    // counts from the device): grids are sized from the capacities
+    G.n_spans = (int32_t)std::min<int64_t>(span_cap, 1 << 30);
     nc::LaunchShape shape = L;
     cudaGraph_t g = nullptr;
     if (dense) nc::prepare_dense_launch();
