@@ -598,23 +598,61 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
     return __double2float_rn(pd);
 }
 
-// Lane per neuron (warp per tile of 32).  Inside its AP (t - lastFire < KC) a neuron's
-// potential comes from the AP table whatever its sum is, and it cannot cross the
-// threshold, so its fold is skipped.
+// Lane per neuron (warp per tile of 32, a block per group of tiles).  Inside its AP
+// (t - lastFire < KC) a neuron's potential comes from the AP table whatever its sum is,
+// and it cannot cross the threshold, so its fold is skipped.  The block's remaining
+// folds are packed onto its first threads before they run: a warp's FP64 add costs the
+// same however few lanes are active, and at saturation two neurons in three are in
+// their AP.
 __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcPools P)
 {
     __shared__ int s_net[kMaxWarps];
     __shared__ unsigned long long s_acc[kMaxWarps][1];
     __shared__ int s_last;
+    __shared__ int s_cnt[kMaxWarps];
+    __shared__ uint16_t s_list[kMaxWarps * 32];
+    __shared__ float s_pot[kMaxWarps * 32];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-    const int nw = gridDim.x * (blockDim.x >> 5);
+    const int wpb = blockDim.x >> 5;
     const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
 
     int acc_net = -1;
     unsigned long long acc[1] = {0};  // fires
-    for (int tix = gw; tix < n_tiles; tix += nw) {
+    for (int tb = blockIdx.x; tb * wpb < n_tiles; tb += gridDim.x) {
+        // which of the block's neurons fold, packed in tile order
+        const int tix = tb * wpb + wib;
+        bool need = false;
+        if (tix < n_tiles) {
+            const NcTile tile = P.tiles[tix];
+            const NcNetDesc& D = P.nets[tile.net];
+            const int32_t t = D.t;
+            const int32_t j = tile.first + lane;
+            if (D.active && t <= D.t_end && j < D.n) {
+                const int32_t lf = P.lf[D.neuron_base + j];
+                need = !(lf != NC_NEVER && t - lf < D.kc) &&
+                       P.in_ptr[D.ptr_base + j + 1] > P.in_ptr[D.ptr_base + j];
+            }
+        }
+        const uint32_t need_m = __ballot_sync(kFull, need);
+        if (lane == 0) s_cnt[wib] = __popc(need_m);
+        __syncthreads();
+        int base = 0, total = 0;
+        for (int w = 0; w < wpb; ++w) {
+            base += w < wib ? s_cnt[w] : 0;
+            total += s_cnt[w];
+        }
+        if (need) s_list[base + __popc(need_m & ((1u << lane) - 1u))] = (uint16_t)(wib * 32 + lane);
+        __syncthreads();
+        for (int r = threadIdx.x; r < total; r += blockDim.x) {
+            const int ent = s_list[r];
+            const NcTile tile = P.tiles[tb * wpb + (ent >> 5)];
+            const NcNetDesc& D = P.nets[tile.net];
+            const int32_t j = tile.first + (ent & 31);
+            s_pot[ent] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
+        }
+        __syncthreads();
+        if (tix >= n_tiles) continue;
         const NcTile tile = P.tiles[tix];
         const NcNetDesc& D = P.nets[tile.net];
         const int32_t t = D.t;
@@ -633,12 +671,11 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
         bool fired = false;
         if (live) {
             int32_t lf = P.lf[pj];
-            float pot = P.pot[pj];
+            float pot = need ? s_pot[wib * 32 + lane] : P.pot[pj];
             const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
             const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
             bool forced = (fw >> lane) & 1u;
             if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
-            if (!(lf != NC_NEVER && t - lf < kc)) pot = fold_row(P, D, j, pot);
             // charge_passive (src/NeuCor.cpp:677-680)
             pot = (pot - -70.0f) * D.leak + -70.0f;
             // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
