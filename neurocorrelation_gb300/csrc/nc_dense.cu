@@ -391,150 +391,155 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
     uint32_t phases = 0u;  // bit j: parity of slot j's next completion
     bool ok = true;
     int qn = 0, nl = 0, nd = 0;
-    for (int k = 0;; ++k) {
-        const int sp = gw + (k / kUnitsPerSpan) * nw;
+    for (int i = 0;; ++i) {
+        const int sp = gw + i * nw;
         if (sp >= n_spans) break;
-        const int half = k % kUnitsPerSpan;
-        const int slot = k % kStages;
-        {
-            // the slot consumed last iteration takes unit k + kStages - 1
-            const int kn = k + kStages - 1, sn = kn % kStages;
-            const int spn = gw + (kn / kUnitsPerSpan) * nw;
-            if (lane == 0) {
-                iss &= ~(1 << sn);
-                if (spn < n_spans && stage_unit(P, spn, kn % kUnitsPerSpan, kFlush, &ws.buf[sn], &ws.bar[sn]))
-                    iss |= 1 << sn;
+        // the span's values, once for its units
+        const NcTile span = P.spans[sp];
+        const NcNetDesc& D = P.nets[span.net];
+        const int32_t t = D.t;
+        const int32_t prev = t - 1;
+        if (span.net != acc_net) {
+            if (acc_net >= 0 && lane == 0) {
+                unsigned long long* st = P.nets[acc_net].stats;
+                atomicAdd(st + 1, acc[0]);
+                atomicAdd(st + 2, acc[1]);
             }
+            acc_net = span.net;
+            acc[0] = acc[1] = 0;
         }
-        const int bits = __shfl_sync(kFull, iss, 0);
-        if ((bits >> slot) & 1) {
-            if (!stage_wait(&ws.bar[slot], (phases >> slot) & 1u)) {
-                if (lane == 0) atomicOr(P.dev_err, NC_DEV_ERR_STAGE_TIMEOUT);
-                ok = false;
-                break;
-            }
-            phases ^= 1u << slot;
-            const StageBuf& B = ws.buf[slot];
-            const NcTile span = P.spans[sp];
-            const NcNetDesc& D = P.nets[span.net];
-            const int32_t t = D.t;
-            const int32_t prev = t - 1;
-            if (span.net != acc_net) {
-                if (acc_net >= 0 && lane == 0) {
-                    unsigned long long* st = P.nets[acc_net].stats;
-                    atomicAdd(st + 1, acc[0]);
-                    atomicAdd(st + 2, acc[1]);
+        const int64_t sb = D.syn_base;
+        const int64_t nsyn = D.n_syn;
+        const int64_t s_span = sb + (int64_t)span.first * 32;
+        const int32_t kc = D.kc;
+        const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
+        const int32_t* lfn = P.lf + D.neuron_base;
+        const float* tab_pre = P.tables + D.table_base;
+        const float* tab_post = tab_pre + D.tab_pre_len;
+#pragma unroll 1
+        for (int half = 0; half < kUnitsPerSpan; ++half) {
+            const int k = i * kUnitsPerSpan + half;
+            const int slot = k % kStages;
+            {
+                // the slot consumed last iteration takes unit k + kStages - 1
+                const int kn = k + kStages - 1, sn = kn % kStages;
+                const int spn = gw + (kn / kUnitsPerSpan) * nw;
+                if (lane == 0) {
+                    iss &= ~(1 << sn);
+                    if (spn < n_spans && stage_unit(P, spn, kn % kUnitsPerSpan, kFlush, &ws.buf[sn], &ws.bar[sn]))
+                        iss |= 1 << sn;
                 }
-                acc_net = span.net;
-                acc[0] = acc[1] = 0;
             }
-            const int64_t sb = D.syn_base;
-            const int64_t nsyn = D.n_syn;
-            const int64_t s_span = sb + (int64_t)span.first * 32;
-            const int32_t kc = D.kc;
-            const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
-            const int32_t* lfn = P.lf + D.neuron_base;
-            const float* tab_pre = P.tables + D.table_base;
-            const float* tab_post = tab_pre + D.tab_pre_len;
-            const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
-            for (int h = 0; h < kUnitChunks; h += kUnroll) {
-                uint32_t fword[kUnroll], ihw[kUnroll];
-                int32_t lfp[kUnroll];
-                bool in[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    const int64_t c = c0 + h + u;
-                    const int q = (h + u) * 32 + lane;
-                    in[u] = c * 32 + lane < nsyn;
-                    fword[u] = 0u;
-                    lfp[u] = NC_NEVER;
-                    ihw[u] = 0u;
-                    if (in[u]) {
-                        fword[u] = fprev[B.pre[q] >> 5];
-                        lfp[u] = lfn[B.post[q]];
-                        ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
-                    }
+            const int bits = __shfl_sync(kFull, iss, 0);
+            if ((bits >> slot) & 1) {
+                if (!stage_wait(&ws.bar[slot], (phases >> slot) & 1u)) {
+                    if (lane == 0) atomicOr(P.dev_err, NC_DEV_ERR_STAGE_TIMEOUT);
+                    ok = false;
+                    break;
                 }
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    const int64_t c = c0 + h + u;
-                    const int q = (h + u) * 32 + lane;
-                    const int64_t s = sb + c * 32 + lane;
-                    const int32_t la = B.la[q];
-                    int32_t lac = in[u] ? la : NC_NEVER;
-                    bool launch = false;
-                    float x = 0.0f;
-                    if (in[u]) {
-                        const uint32_t dl = B.dl[q];
-                        const bool tf = lfp[u] == prev;  // target fired at prev
-                        const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
-                        const bool arrived = la == prev;
-                        const int32_t after = (int32_t)((dl >> 14) & 1u);
-                        launch = srcf && (la == NC_NEVER || prev - la >= kc + after);
-                        nl += launch;
-                        nd += srcf && !launch;
-                        const bool ih = (ihw[u] >> lane) & 1u;
-                        const float w0 = B.w[q];
-                        float w1 = w0;
-                        if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, B.ta[q]), 0.0f, D);
-                        if (launch) {
-                            // target below the source in caller order and fired at prev:
-                            // its update ran first, post-spike plasticity included
-                            const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
-                            // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                            x = D.dt * (D.c52 * cap);
-                            lac = prev + (int32_t)(dl & 0x3fffu);
-                            P.la_c[s] = lac;
+                phases ^= 1u << slot;
+                const StageBuf& B = ws.buf[slot];
+                const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
+                for (int h = 0; h < kUnitChunks; h += kUnroll) {
+                    uint32_t fword[kUnroll], ihw[kUnroll];
+                    int32_t lfp[kUnroll];
+                    bool in[kUnroll];
+    #pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int64_t c = c0 + h + u;
+                        const int q = (h + u) * 32 + lane;
+                        in[u] = c * 32 + lane < nsyn;
+                        fword[u] = 0u;
+                        lfp[u] = NC_NEVER;
+                        ihw[u] = 0u;
+                        if (in[u]) {
+                            fword[u] = fprev[B.pre[q] >> 5];
+                            lfp[u] = lfn[B.post[q]];
+                            ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
                         }
-                        float w2 = w1;
-                        if (arrived) {
-                            w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
-                            P.t_arr[s] = prev;
-                        }
-                        if (tf || arrived) P.w[s] = w2;
                     }
-                    // arrived t-KC .. t-1: in the fold of step t
-                    const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
-                    const uint32_t wm = __ballot_sync(kFull, win);
-                    if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
-                    const uint32_t lm = __ballot_sync(kFull, launch);
-                    if (lm) {
-                        if (launch) {
-                            const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                            ws.qs[pos] = (int32_t)(s - s_span);
-                            ws.qx[pos] = x;
-                        }
-                        qn += __popc(lm);
-                        if (qn >= 32) {
-                            __syncwarp();
-                            P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
-                            __syncwarp();
-                            if (lane < qn - 32) {
-                                ws.qs[lane] = ws.qs[32 + lane];
-                                ws.qx[lane] = ws.qx[32 + lane];
+    #pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int64_t c = c0 + h + u;
+                        const int q = (h + u) * 32 + lane;
+                        const int64_t s = sb + c * 32 + lane;
+                        const int32_t la = B.la[q];
+                        int32_t lac = in[u] ? la : NC_NEVER;
+                        bool launch = false;
+                        float x = 0.0f;
+                        if (in[u]) {
+                            const uint32_t dl = B.dl[q];
+                            const bool tf = lfp[u] == prev;  // target fired at prev
+                            const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
+                            const bool arrived = la == prev;
+                            const int32_t after = (int32_t)((dl >> 14) & 1u);
+                            launch = srcf && (la == NC_NEVER || prev - la >= kc + after);
+                            nl += launch;
+                            nd += srcf && !launch;
+                            const bool ih = (ihw[u] >> lane) & 1u;
+                            const float w0 = B.w[q];
+                            float w1 = w0;
+                            if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, B.ta[q]), 0.0f, D);
+                            if (launch) {
+                                // target below the source in caller order and fired at prev:
+                                // its update ran first, post-spike plasticity included
+                                const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
+                                // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                                x = D.dt * (D.c52 * cap);
+                                lac = prev + (int32_t)(dl & 0x3fffu);
+                                P.la_c[s] = lac;
                             }
-                            __syncwarp();
-                            qn -= 32;
+                            float w2 = w1;
+                            if (arrived) {
+                                w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
+                                P.t_arr[s] = prev;
+                            }
+                            if (tf || arrived) P.w[s] = w2;
+                        }
+                        // arrived t-KC .. t-1: in the fold of step t
+                        const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
+                        const uint32_t wm = __ballot_sync(kFull, win);
+                        if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
+                        const uint32_t lm = __ballot_sync(kFull, launch);
+                        if (lm) {
+                            if (launch) {
+                                const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                                ws.qs[pos] = (int32_t)(s - s_span);
+                                ws.qx[pos] = x;
+                            }
+                            qn += __popc(lm);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                                __syncwarp();
+                                if (lane < qn - 32) {
+                                    ws.qs[lane] = ws.qs[32 + lane];
+                                    ws.qx[lane] = ws.qx[32 + lane];
+                                }
+                                __syncwarp();
+                                qn -= 32;
+                            }
                         }
                     }
                 }
+                // the queue holds offsets into this span: drain it before the warp moves on
+                // to another span (the span's next unit follows when it was issued)
+                const bool more = half + 1 < kUnitsPerSpan && ((bits >> ((k + 1) % kStages)) & 1);
+                if (!more) {
+                    __syncwarp();
+                    if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                    qn = 0;
+                    acc[0] += (unsigned long long)warp_sum(nl);
+                    acc[1] += (unsigned long long)warp_sum(nd);
+                    nl = nd = 0;
+                }
             }
-            // the queue holds offsets into this span: drain it before the warp moves on
-            // to another span (the span's next unit follows when it was issued)
-            const bool more = half + 1 < kUnitsPerSpan && ((bits >> ((k + 1) % kStages)) & 1);
-            if (!more) {
-                __syncwarp();
-                if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
-                qn = 0;
-                acc[0] += (unsigned long long)warp_sum(nl);
-                acc[1] += (unsigned long long)warp_sum(nd);
-                nl = nd = 0;
-            }
+            // the slot is refilled next iteration: finish reading it first, and order those
+            // reads before the copy engine's writes
+            __syncwarp();
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
-        // the slot is refilled next iteration: finish reading it first, and order those
-        // reads before the copy engine's writes
-        __syncwarp();
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (!ok) break;
     }
     if (!ok) {
         // let this warp's copies in flight land (bounded) before the block's shared
