@@ -268,9 +268,11 @@ __global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses_dir
 // on the current one (a ring of stage buffers, one mbarrier each): the memory system
 // sees the copies in flight whatever the warp's registers hold, and 24 warps per SM
 // (8 per block, 3 blocks) cover the compute's own latencies.  Shapes measured on the
-// 100k x 100 network (us per pass): 8 warps / half-span units / 2 stages 103,
-// 6 / whole spans / 2 stages 104, 4 / whole / 2 105, 6 / half / 3 110, 4 / half / 4
-// 119, 4 / whole / 3 136.
+// 100k x 100 network (us per pass, before the span-level values were shared by a
+// span's units): 8 warps / half-span units / 2 stages 103, 6 / whole spans / 2 stages
+// 104, 4 / whole / 2 105, 6 / half / 3 110, 4 / half / 4 119, 4 / whole / 3 136; after:
+// a unit's four chunks gathered together 95.5 against two at a time 99.3, and 3 stages
+// 104.8.
 
 #ifndef NC_STAGE_WARPS
 #define NC_STAGE_WARPS 8
@@ -286,7 +288,11 @@ constexpr int kUnitChunks = NC_STAGE_UNIT;   // chunks per staged unit
 constexpr int kUnitSyn = kUnitChunks * 32;
 constexpr int kUnitsPerSpan = NC_SPAN_CHUNKS / kUnitChunks;
 constexpr int kStages = NC_STAGE_DEPTH;      // units in flight per warp, the current one included
-static_assert(NC_SPAN_CHUNKS % kUnitChunks == 0 && kUnitChunks % kUnroll == 0, "unit shape");
+#ifndef NC_STAGE_UNROLL
+#define NC_STAGE_UNROLL 4
+#endif
+constexpr int kStageUnroll = NC_STAGE_UNROLL;  // chunks whose gathers are in flight together
+static_assert(NC_SPAN_CHUNKS % kUnitChunks == 0 && kUnitChunks % kStageUnroll == 0, "unit shape");
 
 struct StageBuf {                 // one unit, as laid out in the pools (16-byte multiples)
     int32_t pre[kUnitSyn];
@@ -440,12 +446,12 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
                 phases ^= 1u << slot;
                 const StageBuf& B = ws.buf[slot];
                 const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
-                for (int h = 0; h < kUnitChunks; h += kUnroll) {
-                    uint32_t fword[kUnroll], ihw[kUnroll];
-                    int32_t lfp[kUnroll];
-                    bool in[kUnroll];
+                for (int h = 0; h < kUnitChunks; h += kStageUnroll) {
+                    uint32_t fword[kStageUnroll], ihw[kStageUnroll];
+                    int32_t lfp[kStageUnroll];
+                    bool in[kStageUnroll];
     #pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
+                    for (int u = 0; u < kStageUnroll; ++u) {
                         const int64_t c = c0 + h + u;
                         const int q = (h + u) * 32 + lane;
                         in[u] = c * 32 + lane < nsyn;
@@ -459,7 +465,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
                         }
                     }
     #pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
+                    for (int u = 0; u < kStageUnroll; ++u) {
                         const int64_t c = c0 + h + u;
                         const int q = (h + u) * 32 + lane;
                         const int64_t s = sb + c * 32 + lane;
