@@ -35,6 +35,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 namespace {
 
 using namespace nc_dev;
@@ -777,23 +779,29 @@ SynKernel syn_kernel()
 }
 
 // Blocks of the persistent grid on the current device (cached per device; the staged
-// form's shared-memory opt-in is set here, before the first launch).
+// form's shared-memory opt-in is set here, before the first launch).  Returns 0 when
+// the device cannot run the pass (the launch then reports an error).
 template <bool kFlush>
 int resident_blocks()
 {
-    static int cache[64] = {};
+    static std::atomic<int> cache[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-    if (cache[dev] == 0) {
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
         const SynKernel k = syn_kernel<kFlush>();
-        if (k.smem > 48 * 1024)
-            cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+        if (k.smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem) != cudaSuccess)
+            return 0;
         int sms = 0, per_sm = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.threads, k.smem);
-        cache[dev] = sms * per_sm > 0 ? sms * per_sm : 1;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.threads, k.smem) != cudaSuccess ||
+            sms * per_sm <= 0)
+            return 0;
+        n = sms * per_sm;
+        cache[dev].store(n, std::memory_order_relaxed);
     }
-    return cache[dev];
+    return n;
 }
 
 template <bool kFlush>
@@ -802,9 +810,10 @@ int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
     const SynKernel k = syn_kernel<kFlush>();
     const int wpb = k.threads / 32;
     const int full = (P.n_spans + wpb - 1) / wpb;
+    if (full <= 0) return 0;
     const int resident = resident_blocks<kFlush>();
+    if (resident <= 0) return -1;
     const int blocks = L.dense_blocks > 0 ? L.dense_blocks : (full < resident ? full : resident);
-    if (blocks <= 0) return 0;
     k.fn<<<blocks, k.threads, k.smem, s>>>(P);
     return 0;
 }
@@ -815,7 +824,7 @@ namespace nc {
 
 int launch_dense_synapses(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    launch_syn<false>(P, L, (cudaStream_t)stream);
+    if (launch_syn<false>(P, L, (cudaStream_t)stream)) return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -839,7 +848,7 @@ int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream)
 
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream)
 {
-    launch_syn<true>(P, L, (cudaStream_t)stream);
+    if (launch_syn<true>(P, L, (cudaStream_t)stream)) return -1;
     k_dense_mark_flushed<<<1, 256, 0, (cudaStream_t)stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
