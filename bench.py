@@ -374,6 +374,20 @@ def measure_large(G, mode, sim_steps=100, timed=5):
     return out
 
 
+def aggregate_over_ranks(pg, secs, e2e_secs, events, e2e_events):
+    """The whole job's timing and work: the slowest rank's seconds (timed region and end
+    to end) and the events of all ranks.  pg: torch.distributed, or None for one rank."""
+    if not pg:
+        return secs, e2e_secs, events, e2e_events
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([secs, e2e_secs], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    c = torch.tensor([events, e2e_events], dtype=torch.float64, device=dev)
+    pg.all_reduce(c)
+    return float(t[0]), float(t[1]), float(c[0]), float(c[1])
+
+
 def run_ours(args):
     world, rank, local = dist_env()
     pg = None
@@ -445,19 +459,7 @@ def run_ours(args):
     e2e_events = st_e1["launched"] - st_e0["launched"]
 
     # aggregate over ranks
-    secs = ms / 1e3
-    tot_events = events
-    e2e_secs = e2e_wall
-    tot_e2e = e2e_events
-    if pg:
-        import torch
-        dev = "cuda" if torch.cuda.is_available() else "cpu"
-        t = torch.tensor([secs, e2e_secs], dtype=torch.float64, device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        secs, e2e_secs = float(t[0]), float(t[1])
-        c = torch.tensor([tot_events, tot_e2e], dtype=torch.float64, device=dev)
-        pg.all_reduce(c)
-        tot_events, tot_e2e = float(c[0]), float(c[1])
+    secs, e2e_secs, tot_events, tot_e2e = aggregate_over_ranks(pg, ms / 1e3, e2e_wall, events, e2e_events)
     if rank != 0:
         if pg:
             pg.destroy_process_group()
