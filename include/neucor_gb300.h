@@ -377,24 +377,31 @@ int nc_server_fetch(nc_server* server, int64_t request_id, float* weights, float
 int nc_server_get_stats(nc_server* server, nc_server_stats* out);
 int nc_server_destroy(nc_server* server);
 
-/* Advances the network like nc_run, for callers that may not allocate device memory
- * once the network exists: code that records the step into a CUDA graph of its own
- * (allocation is not allowed while a stream is being captured) and services running
- * under a fixed device-memory budget.  nc_run replays CUDA graphs it instantiates on
+/* Advances the network like nc_run, for callers that cannot let the library allocate
+ * device memory once the network exists: a simulation service that reserves a fixed
+ * device-memory budget up front and admits work against it, or a host program (a
+ * renderer, a game or robotics engine embedding the simulator) whose own allocator owns
+ * the GPU's memory.  For them a cudaMalloc made behind their back can fail when the
+ * memory is spoken for, or break their accounting.  nc_run instantiates CUDA graphs on
  * first use and, in the event form (NC_STEP_EVENT), keeps its per-step scratch (the
  * list of neurons that fired, passed from the neuron update to the spike launch) in
  * memory the handle allocated.  This call launches the same kernels directly on
- * `stream` (NULL = the handle's own stream).  The dense form needs no scratch; the
- * event form gets a fixed scratch array compiled into the library instead, so the call
- * allocates nothing.  That array (4 MiB) is held by every GPU that loads the library
- * until the process exits, and it limits event-form calls to networks of at most
- * NC_NOALLOC_MAX_NEURONS neurons; larger ones are refused with NC_ERR_INVALID.  The
- * first event-form call on a device looks the array up (cudaGetSymbolAddress): make it
- * before any stream capture.  All event-form calls share the one array, so calls whose
- * kernels overlap on the GPU (other handles, other streams) race: order them.  Order
- * the call after the handle's earlier work and synchronise `stream` before reading
- * results when it is not the handle's stream.  The reference has no counterpart: its
- * simulator runs on the CPU. */
+ * `stream` (NULL = the handle's own stream) and calls no cudaMalloc, cudaFree or
+ * allocating library routine.  The dense form needs no scratch; the event form uses a
+ * fixed scratch array compiled into the library.  That array (4 MiB) is held by every
+ * GPU that loads the library until the process exits, and it limits event-form calls
+ * to networks of at most NC_NOALLOC_MAX_NEURONS neurons; larger ones are refused with
+ * NC_ERR_INVALID.  The first event-form call on a device looks the array's device
+ * address up (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture.  Every call clears the array's counters before its kernels run; the
+ * array otherwise keeps the last call's contents, and all event-form calls share it,
+ * so calls whose kernels overlap on the GPU (other handles, other streams) race: order
+ * them.  Order the call after the handle's earlier work, and synchronise `stream`
+ * before any other call on the handle when it is not the handle's stream.  After this
+ * call the handle reads its step counter and simulated time back from the device
+ * (nc_get_step, nc_get_time and the read-backs wait for the handle's stream to do so).
+ * The reference has no counterpart: its simulator runs on the CPU and allocates
+ * nothing on a GPU. */
 #define NC_NOALLOC_MAX_NEURONS 262144
 int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream);
 

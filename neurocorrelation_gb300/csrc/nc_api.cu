@@ -42,6 +42,28 @@ float render_behaviour(float val)
         if (e_ != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("cudaSetDevice", e_)); \
     } while (0)
 
+// Host step and time from the device's step counter, for handles advanced by
+// nc_run_noalloc (nc_net::counters_on_device).  Waits for the handle's stream.
+static int refresh_counters(nc_net* net)
+{
+    if (!net->counters_on_device) return NC_OK;
+    std::string err;
+    NcNetDesc d{};
+    int rc = net->eng.sync(err);
+    if (rc == NC_OK) rc = net->eng.read_desc(0, &d, err);
+    if (rc != NC_OK) return fail(rc, err);
+    net->step = (int64_t)d.t - 1;
+    net->time = d.tsum;
+    return NC_OK;
+}
+
+// NC_NEED, then the host counters brought up to date.
+#define NC_NEED_COUNTERS(net)                                         \
+    do {                                                              \
+        NC_NEED(net);                                                 \
+        if (int rc_c_ = refresh_counters(net)) return rc_c_;         \
+    } while (0)
+
 #define NC_TRY(expr)                              \
     do {                                          \
         std::string err_;                         \
@@ -269,7 +291,7 @@ static int upload_firers(nc_net* net, const std::vector<NcFirer>& old, const std
 int nc_set_input_rate_array(nc_net* net, const float* rates_hz, uint32_t count, const float* xyz,
                             const float* radius)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (xyz && !radius) return fail(NC_ERR_INVALID, "positions given without radii");
     if (count > (1u << 24)) return fail(NC_ERR_INVALID, "too many input firers");
     std::vector<NcFirer> old;
@@ -416,7 +438,7 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* ids)
 
 int nc_run(nc_net* net, int32_t n_steps)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (n_steps < 0) return fail(NC_ERR_INVALID, "negative step count");
     if (net->step + n_steps >= (1ll << 30)) return fail(NC_ERR_INVALID, "step counter limit reached");
     NC_CALL(net->eng, step, (int64_t)n_steps);
@@ -429,12 +451,14 @@ int nc_sync(nc_net* net)
 {
     NC_NEED(net);
     NC_CALL0(net->eng, sync);
+    if (int rc = refresh_counters(net)) return rc;
     return NC_OK;
 }
 
 int nc_get_time(nc_net* net, float* ms)
 {
     if (!net || !ms) return fail(NC_ERR_INVALID, "null argument");
+    if (net->counters_on_device) NC_NEED_COUNTERS(net);
     *ms = net->time;
     return NC_OK;
 }
@@ -442,6 +466,7 @@ int nc_get_time(nc_net* net, float* ms)
 int nc_get_step(nc_net* net, int64_t* step)
 {
     if (!net || !step) return fail(NC_ERR_INVALID, "null argument");
+    if (net->counters_on_device) NC_NEED_COUNTERS(net);
     *step = net->step;
     return NC_OK;
 }
@@ -456,7 +481,7 @@ int nc_get_counts(nc_net* net, int32_t* n_neurons, int64_t* n_synapses)
 
 int nc_record_raster(nc_net* net, int32_t max_steps)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (max_steps < 0) return fail(NC_ERR_INVALID, "negative step count");
     NC_CALL0(net->eng, sync);
     net->raster_t0 = (int32_t)net->step + 1;
@@ -485,7 +510,7 @@ int nc_record_raster(nc_net* net, int32_t max_steps)
 
 int nc_read_raster(nc_net* net, uint8_t* out, int64_t capacity_bytes, int32_t* steps)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (!steps) return fail(NC_ERR_INVALID, "null steps");
     const int64_t done = net->step - net->raster_t0 + 1;
     const int32_t rows = (int32_t)std::max<int64_t>(0, std::min<int64_t>(done, net->raster_cap));
@@ -523,7 +548,7 @@ int nc_read_potentials(nc_net* net, float* out_n)
 
 int nc_read_potact(nc_net* net, float* out_2n)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     const int32_t n = net->host.n;
     if (!out_2n && n) return fail(NC_ERR_INVALID, "null output");
     std::vector<float> pot((size_t)n);
@@ -618,7 +643,7 @@ int nc_read_inhibitory(nc_net* net, uint8_t* out_s)
 
 int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t capacity, int64_t* count)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (!count) return fail(NC_ERR_INVALID, "null count");
     const nc::NetHost& h = net->host;
     *count = h.s;
@@ -664,7 +689,7 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
 
 int nc_reset_activities(nc_net* net)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     const auto& sl = net->eng.slots[0];
     std::vector<int32_t> start((size_t)sl.n, (int32_t)net->step);
     cudaError_t e = cudaMemcpyAsync(net->eng.P.act_start + sl.neuron_base, start.data(), sizeof(int32_t) * sl.n,
@@ -705,7 +730,7 @@ int nc_delete_neuron(nc_net* net, int32_t id)
 
 int nc_time_steps(nc_net* net, int32_t n_steps, float* ms, float* kernel_ms)
 {
-    NC_NEED(net);
+    NC_NEED_COUNTERS(net);
     if (n_steps < 0 || !ms) return fail(NC_ERR_INVALID, "bad argument");
     NC_CALL(net->eng, step_timed, (int64_t)n_steps, ms);
     net->step += n_steps;

@@ -9,6 +9,10 @@ struct nc_net {
     nc::Engine eng;
     int64_t step = 0;      // completed steps
     float time = 0.0f;     // NeuCor::currentTime, accumulated per step
+    // Set by nc_run_noalloc: its launches may run again without this handle seeing
+    // them, so from then on step and time are read back from the device's step
+    // counter (NcNetDesc t, tsum) before any call that uses them.
+    bool counters_on_device = false;
     uint32_t* d_raster = nullptr;
     uint32_t* d_raster_ids = nullptr;  // the same rows in caller-id order (read-back staging)
     int32_t raster_cap = 0;

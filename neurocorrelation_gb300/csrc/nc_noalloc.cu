@@ -1,14 +1,17 @@
 // nc_noalloc.cu — nc_run_noalloc (neucor_gb300.h): the simulation step for callers
-// that must not allocate device memory once their network is set up.
+// that cannot let the library allocate device memory once their network is set up.
 //
-// nc_run keeps the compacted list of neurons that fired in a step — the scratch the
-// neuron-update kernel writes and the spike-launch kernel reads — in memory the handle
-// allocated, and replays CUDA graphs it instantiates on first use.  Code that records
-// the step into its own CUDA graph, or runs under a fixed device-memory budget, cannot
-// let the library allocate or instantiate anything per call.  nc_run_noalloc launches
-// the same kernels directly.  The event form gets a scratch area that lives in this
-// file's static device array instead; the dense form needs none.  Nothing is
-// allocated, the network's own arrays are the inputs and outputs.
+// Some callers own every byte of device memory themselves: a simulation service that
+// reserves a fixed budget per GPU up front and admits work against it, or a host
+// program (a renderer, a game or robotics engine embedding the simulator) whose own
+// allocator has carved up the GPU.  A cudaMalloc made behind their back can fail when
+// the memory is spoken for, or silently break their accounting.  nc_run keeps the
+// compacted list of neurons that fired in a step — the scratch the neuron-update kernel
+// writes and the spike-launch kernel reads — in memory the handle allocated, and
+// instantiates CUDA graphs (which allocate) on first use.  nc_run_noalloc launches the
+// same kernels directly.  The event form gets its scratch from this file's static
+// device array instead; the dense form needs none.  Nothing is allocated: the
+// network's own arrays are the inputs and outputs.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -98,5 +101,8 @@ extern "C" int nc_run_noalloc(nc_net* net, int32_t n_steps, void* stream)
     }
     net->step += n_steps;
     for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;
+    // the launches above are not tracked by the handle once issued: later calls on the
+    // handle read the step counter and simulated time back from the device
+    net->counters_on_device = true;
     return NC_OK;
 }

@@ -134,6 +134,11 @@ void ncs_background_draws(uint64_t seed, int32_t n, float dt, int32_t counter, u
 /* Delay in steps for a synapse of the given length (see nc_oracle.c). */
 int32_t ncs_delay_steps(float length, float dt);
 
+/* The workloads' kNN network (nc_knn.c): positions (3n floats) and n*k synapses by
+ * source then rank; the same network as the library's nc_build_knn.  0 on success. */
+int ncs_build_knn(int32_t n, int32_t k, float density, uint64_t seed, int32_t threads, float* xyz,
+                  int32_t* syn_from, int32_t* syn_to, float* syn_weight);
+
 #ifdef __cplusplus
 }
 #endif

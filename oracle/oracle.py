@@ -66,11 +66,17 @@ class Stats(ctypes.Structure):
 _lib = None
 
 
+def reference_dir() -> str:
+    """The reference's source tree: $NEUCOR_REF_DIR when set, else a `reference`
+    directory beside this repository's root (absent on machines without it)."""
+    return os.environ.get("NEUCOR_REF_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def build(quiet: bool = True) -> None:
     """Compile liboracle_s.so (and _ref/neucor_ref when the reference tree exists)."""
     args = ["make", "-s", "-C", HERE, "all"]
     subprocess.run(args, check=True, capture_output=quiet)
-    if os.path.isdir("/root/reference/src"):
+    if os.path.isdir(os.path.join(reference_dir(), "src")):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, capture_output=quiet)
 
 
@@ -110,6 +116,9 @@ def lib() -> ctypes.CDLL:
         L.ncs_input_fires.argtypes = [P, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float, ctypes.c_int32, P,
                                       ctypes.c_int32]
         L.ncs_background_draws.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_float, ctypes.c_int32, P, P]
+        L.ncs_build_knn.restype = ctypes.c_int32
+        L.ncs_build_knn.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_uint64, ctypes.c_int32,
+                                    P, P, P, P]
         L.ncs_delay_steps.restype = ctypes.c_int32
         L.ncs_delay_steps.argtypes = [ctypes.c_float, ctypes.c_float]
         _lib = L
@@ -253,6 +262,21 @@ class OracleS:
         return {f: getattr(s, f) for f, _ in Stats._fields_}
 
 
+def build_knn(n: int, k: int, density: float = 8.0, seed: int = 0, threads: int = 0):
+    """The workloads' kNN network (nc_knn.c): xyz (n, 3), and per synapse (source, then
+    rank) pre, post, weight — the network the library's nc_build_knn makes."""
+    threads = threads or (os.cpu_count() or 1)
+    xyz = np.zeros((n, 3), dtype=np.float32)
+    pre = np.zeros(n * k, dtype=np.int32)
+    post = np.zeros(n * k, dtype=np.int32)
+    w = np.zeros(n * k, dtype=np.float32)
+    rc = lib().ncs_build_knn(int(n), int(k), float(density), int(seed), int(threads), _ptr(xyz), _ptr(pre),
+                             _ptr(post), _ptr(w))
+    if rc != 0:
+        raise ValueError(f"ncs_build_knn failed ({rc})")
+    return xyz, pre, post, w
+
+
 def input_fires(groups, seed: int, dt: float, t: int):
     g = groups_array(groups)
     cap = sum(int(x["count"]) for x in groups) + 1
@@ -269,7 +293,7 @@ def background_draws(seed: int, n: int, dt: float, counter: int):
 
 
 # ------------------------------------------------------------- Oracle-R runner
-MODES = {"canonical": 0, "native": 1, "continuous": 2, "construct": 4}
+MODES = {"canonical": 0, "native": 1, "continuous": 2, "continuous_grid": 3, "construct": 4}
 
 
 def reference_available() -> bool:

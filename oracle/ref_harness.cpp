@@ -23,10 +23,13 @@
 //                  at the new T so each step ends with all neurons updated.
 //   2 continuous — NeuCor::run alone, synapse lengths as constructed (spikes
 //                  arrive between steps), background firing from glibc rand().
+//   3 continuous on the step grid — as 2, with every synapse length set to its
+//                  whole-step delay (separates the effect of delay rounding from
+//                  that of the off-grid background fire times).
 //   4 construct  — srand(seed); NeuCor(n) (NeuCor.cpp:17-42); writes the positions
 //                  and every synapse (source, target, weight, length) in the
 //                  reference's own order.
-// Modes 0 and 1 set every synapse length to delay*dt/AP_speed so spikes arrive
+// Modes 0, 1 and 3 set every synapse length to delay*dt/AP_speed so spikes arrive
 // on the step grid.
 #include "NeuCor.h"
 #include "nc_oracle.h"
@@ -223,7 +226,7 @@ public:
             uint8_t* rr = &raster[row * (size_t)(t - 1)];
             for (int32_t j = 0; j < n; ++j) {
                 const float lf = brain_->neurons[j].lastFire;
-                bool fired = sc_.mode == 2 ? (lf == lf && lf > T - dt && lf <= T) : (lf == T);
+                bool fired = (sc_.mode == 2 || sc_.mode == 3) ? (lf == lf && lf > T - dt && lf <= T) : (lf == T);
                 if (fired) rr[j >> 3] |= (uint8_t)(1u << (j & 7));
                 if (sc_.record_pot) pots[(size_t)(t - 1) * n + j] = brain_->potAct[2 * (size_t)j];
             }

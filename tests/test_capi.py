@@ -92,3 +92,23 @@ def test_unsupported_operations_are_reported(nc):
     lib = nc.load_library()
     assert lib.nc_delete_synapse(None, 0, 1) == -4
     assert lib.nc_delete_neuron(None, 0) == -4
+
+
+@pytest.mark.parametrize("n,k,seed", [(300, 299, 1), (2000, 30, 5), (1000, 50, 1), (20000, 100, 7)])
+def test_oracle_knn_builder_equals_library_builder(nc, oracle_mod, n, k, seed):
+    """The oracle's own kNN restatement (oracle/nc_knn.c, used where the library must not
+    be loaded) and the library's host builder make the same network, bit for bit."""
+    a = oracle_mod.build_knn(n, k, 8.0, seed)
+    b = nc.build_knn(n, k, 8.0, seed=seed)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint32) if x.dtype == np.float32 else x,
+                                      y.view(np.uint32) if y.dtype == np.float32 else y)
+
+
+def test_oracle_knn_builder_matches_brute_force(oracle_mod):
+    n, k = 500, 20
+    xyz, pre, post, w = oracle_mod.build_knn(n, k, 8.0, 3)
+    d = np.sqrt(((xyz[:, None, :] - xyz[None, :, :]) ** 2).sum(-1, dtype=np.float32)).astype(np.float32)
+    np.fill_diagonal(d, np.inf)
+    for i in range(n):
+        np.testing.assert_array_equal(post[i * k:(i + 1) * k], np.lexsort((np.arange(n), d[i]))[:k])

@@ -1,11 +1,14 @@
-"""nc_run_noalloc — the step for callers that may not allocate device memory once the
-network is set up (code recording the step into its own CUDA graph, where allocation is
-not allowed during stream capture; services with a fixed device-memory budget).
+"""nc_run_noalloc — the step for callers that cannot let the library allocate device
+memory once the network is set up: a service that reserves a fixed device budget up
+front and admits work against it, or a host program whose own allocator owns the GPU's
+memory (an engine embedding the simulator), where an allocation behind its back can
+fail or break its accounting.
 
 It launches the same kernels as nc_run (the event form with its per-step scratch in a
 static device array; the dense form needs none), so it must compute exactly what nc_run
 computes; checked on two calls in a row in both forms, bit for bit (the tolerance of
-every parity test here), through the C ABI."""
+every parity test here), through the C ABI, on the handle's stream and on a stream the
+caller owns."""
 import ctypes
 
 import numpy as np
@@ -38,6 +41,40 @@ def make_pair(G, mode):
 
 def bits(a):
     return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def caller_stream():
+    """A CUDA stream the caller owns (created outside the library)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch has no CUDA device")
+    return torch, torch.cuda.Stream(device=0)
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["dense", "event"])
+def test_noalloc_on_a_caller_stream(nc, mode):
+    """Two calls on a stream the caller created; the caller synchronises it before
+    reading, and the handle's step and time follow the device."""
+    run_noalloc, L = noalloc_fn(nc)
+    torch, stream = caller_stream()
+    ref, na = make_pair(nc, mode)
+    for call in range(2):
+        ref.record_raster(90)
+        na.record_raster(90)
+        ref.run(90)
+        na.sync()  # the handle's earlier work (the raster set-up) before the caller's stream
+        rc = run_noalloc(na._handle(), 90, ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, L.nc_last_error().decode()
+        stream.synchronize()
+        np.testing.assert_array_equal(na.raster(), ref.raster())
+        np.testing.assert_array_equal(bits(na.potentials()), bits(ref.potentials()))
+        np.testing.assert_array_equal(bits(na.weights()), bits(ref.weights()))
+        np.testing.assert_array_equal(bits(na.potAct), bits(ref.potAct))
+        sa, sr = na.stats(), ref.stats()
+        assert (sa["fires"], sa["launched"], sa["dropped"], sa["steps"]) == \
+            (sr["fires"], sr["launched"], sr["dropped"], sr["steps"])
+        assert na.step == ref.step == 90 * (call + 1)
+        assert np.float32(na.getTime()).view(np.uint32) == np.float32(ref.getTime()).view(np.uint32)
 
 
 @pytest.mark.parametrize("mode", [0, 1], ids=["dense", "event"])
