@@ -42,6 +42,7 @@ namespace {
 using namespace nc_dev;
 
 constexpr int kMaxWarps = 8;  // 256 threads per block at most
+
 #ifndef NC_DENSE_UNROLL
 #define NC_DENSE_UNROLL 2
 #endif
@@ -53,6 +54,18 @@ struct SynShared {
     int32_t qs[kMaxWarps][kQueue];  // launched synapse, relative to its span's first
     float qx[kMaxWarps][kQueue];    // deltaT * AP_depolFac of the launch
 };
+
+// Programmatic dependent launch: each pass of the dense step is launched so that its
+// blocks may be scheduled while the previous pass drains, and waits here, before it
+// reads anything, until that pass has completed and its writes are visible.  (A kernel
+// launched without the attribute passes the wait at once.)
+#ifndef NC_PDL
+#define NC_PDL 1
+#endif
+__device__ __forceinline__ void wait_previous_pass()
+{
+    if (NC_PDL) asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 __device__ __forceinline__ int warp_sum(int v)
 {
@@ -226,6 +239,7 @@ __global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses_dir
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
     const int nw = gridDim.x * (blockDim.x >> 5);
+    wait_previous_pass();
     const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
 
     int acc_net = -1;
@@ -375,7 +389,6 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * kStageWarps + wib;
     const int nw = gridDim.x * kStageWarps;
-    const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
     WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[wib];
 
     if (lane == 0) {
@@ -384,6 +397,8 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
+    wait_previous_pass();
+    const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
 
     // unit k of this warp: half k % kUnitsPerSpan of span gw + (k / kUnitsPerSpan) * nw,
     // staged in slot k % kStages
@@ -628,6 +643,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
+    wait_previous_pass();
     const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
 
     int acc_net = -1;
@@ -804,6 +820,22 @@ int resident_blocks()
     return n;
 }
 
+// Launches fn<<<grid, block, smem, s>>>(P) as a programmatic dependent launch.
+cudaError_t launch_pdl(void (*fn)(NcPools), int grid, int block, size_t smem, cudaStream_t s, const NcPools& P)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = NC_PDL ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, fn, P);
+}
+
 template <bool kFlush>
 int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
 {
@@ -814,8 +846,7 @@ int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
     const int resident = resident_blocks<kFlush>();
     if (resident <= 0) return -1;
     const int blocks = L.dense_blocks > 0 ? L.dense_blocks : (full < resident ? full : resident);
-    k.fn<<<blocks, k.threads, k.smem, s>>>(P);
-    return 0;
+    return launch_pdl(k.fn, blocks, k.threads, k.smem, s, P) == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace
@@ -832,7 +863,8 @@ int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
 {
     const int wpb = L.neuron_block / 32;
     const int blocks = (P.n_tiles + wpb - 1) / wpb;
-    if (blocks > 0) k_dense_neurons<<<blocks, L.neuron_block, 0, (cudaStream_t)stream>>>(P);
+    if (blocks > 0 && launch_pdl(k_dense_neurons, blocks, L.neuron_block, 0, (cudaStream_t)stream, P) != cudaSuccess)
+        return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

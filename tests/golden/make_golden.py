@@ -5,7 +5,7 @@ its sources by oracle/Makefile — on small seeded scenarios and stores inputs a
 outputs.  Needs the reference tree (this script does not run on the GPU machines;
 its outputs are committed).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [base] [c1_stats]
 """
 import os
 import sys
@@ -48,10 +48,54 @@ def scenario(name, mode, net, params, groups, steps, extra=(), record_pot=True, 
          **{"p_" + k: v for k, v in params_dict(params).items()})
 
 
-def main():
+C1_SEEDS = (2024, 7, 99)
+
+
+def c1_workload():
+    """1,000 neurons uniform in a cube, 50 nearest targets each, U[0,1) weights (the
+    oracle's kNN restatement, seed 1); 20 inputs at 20 Hz: a correlated group of 10
+    (shared source, +-2-step jitter) and an uncorrelated control group of 10."""
+    xyz, pre, post, w = O.build_knn(1000, 50, 8.0, 1)
+    groups = [dict(first=0, count=10, rate_hz=20.0, correlated=1, jitter=2),
+              dict(first=10, count=10, rate_hz=20.0, correlated=0, jitter=0)]
+    return xyz, pre, post, w, groups
+
+
+def c1_stats(mode, seed, steps=10000, window=1000):
+    """Population statistics of the reference's own NeuCor::run on the C1 workload."""
+    xyz, pre, post, w, groups = c1_workload()
+    ck = list(range(window, steps + 1, window))
+    r = O.run_reference(mode, xyz, pre, post, w, O.default_params(seed=seed), groups=groups, steps=steps,
+                        checkpoints=ck)
+    ras = O.unpack_raster(r["raster"], xyz.shape[0])
+    pop = ras.reshape(steps // window, window, -1).sum((1, 2)) / (xyz.shape[0] * window / 1000.0)
+    wq = np.rint(np.clip(r["weights"], 0.0, 1.0) * 65535.0).astype(np.uint16)  # every 1,000 steps
+    return dict(pop_rate_hz=pop.astype(np.float64), counts=ras.sum(0).astype(np.int32), weights_u16=wq)
+
+
+def c1_statistics():
+    """F. C1 for its 10,000 steps through the reference's own NeuCor::run.
+    native: runAll, synapse lengths on the step grid (the benchmark spec's whole-step
+    delays), background fire times on the step grid; three simulation seeds.
+    continuous: the unmodified timing (lengths as built, glibc rand() background at
+    random times inside the step); one seed."""
+    out = {}
+    for seed in C1_SEEDS:
+        for k, v in c1_stats("native", seed).items():
+            out[f"native_{seed}_{k}"] = v
+    for k, v in c1_stats("continuous", C1_SEEDS[0]).items():
+        out[f"continuous_{C1_SEEDS[0]}_{k}"] = v
+    save("c1_reference_stats", seeds=np.asarray(C1_SEEDS), steps=np.asarray(10000), window=np.asarray(1000), **out)
+
+
+def main(sections):
     if not O.reference_available():
         O.build()
     assert O.reference_available(), "needs the reference tree to build oracle/_ref"
+    if "c1_stats" in sections:
+        c1_statistics()
+    if "base" not in sections:
+        return
 
     # A. FEW_NEURONS preset through the reference's own API (src/main.cpp:162-189):
     # 3 neurons, synapses 0->1, 0->2 at 0.5, periodic inputs at 50 Hz offset 0/+2/-2 ms,
@@ -112,4 +156,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or ["base", "c1_stats"])

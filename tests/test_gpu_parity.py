@@ -183,25 +183,3 @@ def test_gpu_c1_full_horizon_bit_exact(nc, oracle_mod, mode):
     assert_bits_equal(net.potAct[1::2], o.activity(), "activity")
     st, so = net.stats(), o.stats()
     assert (st["fires"], st["launched"], st["dropped"]) == (so["fires"], so["launched"], so["dropped"])
-
-
-@pytest.mark.parametrize("mode", MODES)
-def test_gpu_c2_prefix_bit_exact(nc, oracle_mod, mode):
-    """The 100k-neuron / 10M-synapse workload (200 inputs in 10 groups at 5-40 Hz): the
-    first 300 steps bit-exact against the oracle."""
-    G, O = nc, oracle_mod
-    xyz, pre, post, w = G.build_knn(100000, 100, 8.0, seed=7)
-    rates = np.linspace(5.0, 40.0, 10)
-    groups = [dict(first=20 * g, count=20, rate_hz=float(rates[g]), correlated=1, jitter=2) for g in range(10)]
-    pkw = dict(seed=99)
-    steps = 300
-    net = gpu_net(G, xyz, pre, post, w, dict(pkw, step_mode=MODES[mode]), groups)
-    net.record_raster(steps)
-    net.run(steps)
-    o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw), groups=groups)
-    ro, _ = o.run(steps, raster=True)
-    np.testing.assert_array_equal(net.raster(), ro)
-    assert_bits_equal(net.potentials(), o.potentials(), "potentials")
-    assert_bits_equal(net.weights(), o.weights(), "weights")
-    st, so = net.stats(), o.stats()
-    assert (st["fires"], st["launched"], st["dropped"]) == (so["fires"], so["launched"], so["dropped"])
