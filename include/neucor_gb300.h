@@ -121,6 +121,16 @@ typedef struct {
     int32_t inhibitory;
 } nc_synapse_snapshot;
 
+/* One periodic input firer: NeuCor::InputSnapshot (src/NeuCor.h:56-62,
+ * src/NeuCor.cpp:136-152). */
+typedef struct {
+    int32_t id;
+    float x, y, z;       /* InputFirer::a */
+    float radius;        /* InputFirer::radius */
+    float frequency;     /* its entry of the rate array (0 past the array's end), Hz */
+    int32_t enabled;     /* InputFirer::enabled: always 1 (the reference never clears it) */
+} nc_input_snapshot;
+
 /* ---------------------------------------------------------------- errors */
 const char* nc_last_error(void);
 const char* nc_version(void);
@@ -223,6 +233,9 @@ int nc_read_inhibitory(nc_net* net, uint8_t* out_s);
 /* NeuCor::getSynapseSnapshots (src/NeuCor.cpp:115-134), one entry per kept
  * synapse in source-then-creation order (the reference's outSynapses order). */
 int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t capacity, int64_t* count);
+/* NeuCor::getInputSnapshots (src/NeuCor.cpp:136-152): one record per periodic input firer,
+ * in firer order.  *count receives the number of firers; out may be NULL to query it. */
+int nc_read_input_snapshots(nc_net* net, nc_input_snapshot* out, int32_t capacity, int32_t* count);
 /* NeuCor::resetActivities (src/NeuCor.cpp:233-235). */
 int nc_reset_activities(nc_net* net);
 int nc_get_stats(nc_net* net, nc_stats* out);

@@ -231,6 +231,27 @@ public:
             out[i] = NeuronSnapshot{i, coord3{xyz_[3 * i], xyz_[3 * i + 1], xyz_[3 * i + 2]}, pa[2 * i], pa[2 * i + 1]};
         return out;
     }
+    struct InputSnapshot {        // src/NeuCor.h:56-62
+        std::size_t id;
+        coord3 position;
+        float radius;
+        float frequency;
+        bool enabled;
+    };
+    std::vector<InputSnapshot> getInputSnapshots()       // src/NeuCor.cpp:136-152
+    {
+        materialize();
+        push_rates();
+        int32_t n = 0;
+        check(nc_read_input_snapshots(net_, nullptr, 0, &n));
+        std::vector<nc_input_snapshot> raw((size_t)n);
+        if (n) check(nc_read_input_snapshots(net_, raw.data(), n, &n));
+        std::vector<InputSnapshot> out;
+        out.reserve(raw.size());
+        for (const auto& r : raw)
+            out.push_back(InputSnapshot{(std::size_t)r.id, coord3{r.x, r.y, r.z}, r.radius, r.frequency, r.enabled != 0});
+        return out;
+    }
     std::vector<SynapseSnapshot> getSynapseSnapshots()    // src/NeuCor.cpp:115-134
     {
         materialize();

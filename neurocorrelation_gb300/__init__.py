@@ -67,6 +67,11 @@ class SynapseSnapshotC(ctypes.Structure):
                 ("pre_potential", ctypes.c_float), ("post_potential", ctypes.c_float), ("inhibitory", ctypes.c_int32)]
 
 
+class InputSnapshotC(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int32), ("x", ctypes.c_float), ("y", ctypes.c_float), ("z", ctypes.c_float),
+                ("radius", ctypes.c_float), ("frequency", ctypes.c_float), ("enabled", ctypes.c_int32)]
+
+
 class NetSpec(ctypes.Structure):
     _fields_ = [("n_neurons", ctypes.c_int32), ("xyz", ctypes.c_void_p), ("n_synapses", ctypes.c_int64),
                 ("syn_from", ctypes.c_void_p), ("syn_to", ctypes.c_void_p), ("syn_weight", ctypes.c_void_p),
@@ -112,6 +117,7 @@ def load_library() -> ctypes.CDLL:
         "nc_read_last_fire": ([P, P], I32), "nc_read_weights": ([P, P], I32), "nc_read_delays": ([P, P], I32),
         "nc_read_inhibitory": ([P, P], I32),
         "nc_read_synapse_snapshots": ([P, P, I64, P], I32), "nc_reset_activities": ([P], I32),
+        "nc_read_input_snapshots": ([P, P, I32, P], I32),
         "nc_get_stats": ([P, P], I32), "nc_delete_synapse": ([P, I32, I32], I32),
         "nc_delete_neuron": ([P, I32], I32),
         "nc_build_knn": ([I32, I32, F, ctypes.c_uint64, P, P, P, P], I32),
@@ -222,6 +228,15 @@ class SynapseSnapshot:      # NeuCor::SynapseSnapshot (src/NeuCor.h:45-54)
     prePotential: float
     postPotential: float
     inhibitory: bool
+
+
+@dataclass
+class InputSnapshot:        # NeuCor::InputSnapshot (src/NeuCor.h:56-62)
+    id: int
+    position: tuple
+    radius: float
+    frequency: float
+    enabled: bool
 
 
 class NeuCor:
@@ -557,6 +572,18 @@ class NeuCor:
         return [SynapseSnapshot(s.from_id, s.to_id, tuple(map(float, pos[s.from_id])), tuple(map(float, pos[s.to_id])),
                                 float(s.weight), float(s.pre_potential), float(s.post_potential), bool(s.inhibitory))
                 for s in self.synapse_snapshot_array()]
+
+    def getInputSnapshots(self):
+        """NeuCor::getInputSnapshots (src/NeuCor.cpp:136-152)."""
+        h = self._handle()
+        cnt = ctypes.c_int32()
+        _check(self._lib.nc_read_input_snapshots(h, None, 0, ctypes.byref(cnt)))
+        arr = (InputSnapshotC * max(1, cnt.value))()
+        if cnt.value:
+            _check(self._lib.nc_read_input_snapshots(h, ctypes.cast(arr, ctypes.c_void_p), cnt.value,
+                                                     ctypes.byref(cnt)))
+        return [InputSnapshot(int(r.id), (float(r.x), float(r.y), float(r.z)), float(r.radius), float(r.frequency),
+                              bool(r.enabled)) for r in arr[:cnt.value]]
 
     def resetActivities(self):
         _check(self._lib.nc_reset_activities(self._handle()))

@@ -687,6 +687,29 @@ int nc_read_synapse_snapshots(nc_net* net, nc_synapse_snapshot* out, int64_t cap
     return NC_OK;
 }
 
+int nc_read_input_snapshots(nc_net* net, nc_input_snapshot* out, int32_t capacity, int32_t* count)
+{
+    NC_NEED(net);
+    if (!count) return fail(NC_ERR_INVALID, "null count");
+    const int32_t nf = (int32_t)net->firer_near.size();
+    *count = nf;
+    if (!out || nf == 0) return NC_OK;
+    if (capacity < nf) return fail(NC_ERR_INVALID, "input snapshot buffer too small");
+    std::vector<NcFirer> f;  // the rates as the next step's run call reads them
+    NC_CALL(net->eng, read_firers, f);
+    for (int32_t i = 0; i < nf; ++i) {
+        nc_input_snapshot& o = out[i];
+        o.id = i;
+        o.x = net->firer_xyz[3 * (size_t)i];
+        o.y = net->firer_xyz[3 * (size_t)i + 1];
+        o.z = net->firer_xyz[3 * (size_t)i + 2];
+        o.radius = net->firer_radius[(size_t)i];
+        o.frequency = (size_t)i < f.size() ? f[(size_t)i].rate : 0.0f;
+        o.enabled = 1;
+    }
+    return NC_OK;
+}
+
 int nc_reset_activities(nc_net* net)
 {
     NC_NEED_COUNTERS(net);

@@ -319,8 +319,19 @@ struct StageBuf {                 // one unit, as laid out in the pools (16-byte
     uint16_t dl[kUnitSyn];
 };
 
+struct NetConst {                 // a span's net constants (see the staged pass)
+    const uint32_t* fprev;        // fired bits of prev
+    const float* pst;             // per neuron: post trace at prev, -0.0 when it fired at prev
+    const float* tab_pre;         // presynaptic trace table
+    double e_term;
+    int32_t t, kc, tab_pre_len;
+    float dt, c52;
+    Rates R;
+};
+
 struct __align__(16) WarpStage {
     StageBuf buf[kStages];
+    NetConst nc;
     unsigned long long bar[kStages];  // mbarriers: the copies of buf[k] have landed
     int32_t qs[kQueue];               // launched synapse, relative to its span's first
     float qx[kQueue];
@@ -409,7 +420,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
             if (sp < n_spans && stage_unit(P, sp, k % kUnitsPerSpan, kFlush, &ws.buf[k], &ws.bar[k])) iss |= 1 << k;
         }
 
-    int acc_net = -1;
+    int acc_net = -1, cur_net = -1;
     unsigned long long acc[2] = {0, 0};  // launched, dropped
     uint32_t phases = 0u;  // bit j: parity of slot j's next completion
     bool ok = true;
@@ -434,11 +445,27 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
         const int64_t sb = D.syn_base;
         const int64_t nsyn = D.n_syn;
         const int64_t s_span = sb + (int64_t)span.first * 32;
-        const int32_t kc = D.kc;
-        const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
-        const int32_t* lfn = P.lf + D.neuron_base;
-        const float* tab_pre = P.tables + D.table_base;
-        const float* tab_post = tab_pre + D.tab_pre_len;
+        if (span.net != cur_net) {
+            // the net's constants, once per warp in shared memory: reading them there needs
+            // no reload after each global store (which could alias the descriptor) and no
+            // registers across the chunk loop
+            if (lane == 0) {
+                NetConst& c = ws.nc;
+                c.fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
+                c.pst = P.pst + D.neuron_base;
+                c.tab_pre = P.tables + D.table_base;
+                c.e_term = D.e_term;
+                c.t = t;
+                c.kc = D.kc;
+                c.tab_pre_len = D.tab_pre_len;
+                c.dt = D.dt;
+                c.c52 = D.c52;
+                c.R = rates_of(D);
+            }
+            __syncwarp();
+            cur_net = span.net;
+        }
+        const NetConst& C = ws.nc;
 #pragma unroll 1
         for (int half = 0; half < kUnitsPerSpan; ++half) {
             const int k = i * kUnitsPerSpan + half;
@@ -462,78 +489,86 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
                 }
                 phases ^= 1u << slot;
                 const StageBuf& B = ws.buf[slot];
+                // this unit's synapses start at ubase; offsets within it are 32-bit
                 const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
+                const int64_t ubase = sb + c0 * 32;
+                const int32_t u_rem = (int32_t)min((int64_t)kUnitSyn, nsyn - c0 * 32);  // synapses in the unit
+                int32_t* la_u = P.la_c + ubase;
+                float* w_u = P.w + ubase;
+                int32_t* ta_u = P.t_arr + ubase;
+                uint32_t* win_u = P.win + (ubase >> 5);
+                const uint32_t* inh_u = P.inh + (ubase >> 5);
+                const int32_t qoff = half * kUnitSyn;  // the unit's first synapse, relative to the span
+                const int32_t prev_c = C.t - 1;
                 for (int h = 0; h < kUnitChunks; h += kStageUnroll) {
                     uint32_t fword[kStageUnroll], ihw[kStageUnroll];
-                    int32_t lfp[kStageUnroll];
-                    bool in[kStageUnroll];
+                    float pstv[kStageUnroll];
     #pragma unroll
                     for (int u = 0; u < kStageUnroll; ++u) {
-                        const int64_t c = c0 + h + u;
                         const int q = (h + u) * 32 + lane;
-                        in[u] = c * 32 + lane < nsyn;
                         fword[u] = 0u;
-                        lfp[u] = NC_NEVER;
+                        pstv[u] = 0.0f;
                         ihw[u] = 0u;
-                        if (in[u]) {
-                            fword[u] = fprev[B.pre[q] >> 5];
-                            lfp[u] = lfn[B.post[q]];
-                            ihw[u] = __ldg(P.inh + ((sb >> 5) + c));
+                        if (q < u_rem) {
+                            fword[u] = C.fprev[B.pre[q] >> 5];
+                            pstv[u] = C.pst[B.post[q]];
+                            ihw[u] = __ldg(inh_u + h + u);
                         }
                     }
     #pragma unroll
                     for (int u = 0; u < kStageUnroll; ++u) {
-                        const int64_t c = c0 + h + u;
                         const int q = (h + u) * 32 + lane;
-                        const int64_t s = sb + c * 32 + lane;
+                        const bool in = q < u_rem;
                         const int32_t la = B.la[q];
-                        int32_t lac = in[u] ? la : NC_NEVER;
+                        int32_t lac = in ? la : NC_NEVER;
                         bool launch = false;
                         float x = 0.0f;
-                        if (in[u]) {
+                        if (in) {
                             const uint32_t dl = B.dl[q];
-                            const bool tf = lfp[u] == prev;  // target fired at prev
+                            // target fired at prev: the sign of its post state
+                            const bool tf = __float_as_uint(pstv[u]) == 0x80000000u;
                             const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
-                            const bool arrived = la == prev;
+                            const bool arrived = la == prev_c;
                             const int32_t after = (int32_t)((dl >> 14) & 1u);
-                            launch = srcf && (la == NC_NEVER || prev - la >= kc + after);
+                            launch = srcf && (la == NC_NEVER || prev_c - la >= C.kc + after);
                             nl += launch;
                             nd += srcf && !launch;
                             const bool ih = (ihw[u] >> lane) & 1u;
                             const float w0 = B.w[q];
                             float w1 = w0;
-                            if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, B.ta[q]), 0.0f, D);
+                            if (tf) w1 = plasticity(w0, ih, trace_at(C.tab_pre, C.tab_pre_len, prev_c, B.ta[q]), 0.0f, C.R);
                             if (launch) {
                                 // target below the source in caller order and fired at prev:
                                 // its update ran first, post-spike plasticity included
                                 const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
                                 // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                                x = D.dt * (D.c52 * cap);
-                                lac = prev + (int32_t)(dl & 0x3fffu);
-                                P.la_c[s] = lac;
+                                x = C.dt * (C.c52 * cap);
+                                lac = prev_c + (int32_t)(dl & 0x3fffu);
+                                la_u[q] = lac;
                             }
                             float w2 = w1;
                             if (arrived) {
-                                w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
-                                P.t_arr[s] = prev;
+                                // the target's post trace at prev (0 when it fired at prev)
+                                w2 = plasticity(w1, ih, 0.0f, fabsf(pstv[u]), C.R);
+                                ta_u[q] = prev_c;
                             }
-                            if (tf || arrived) P.w[s] = w2;
+                            if (tf || arrived) w_u[q] = w2;
                         }
                         // arrived t-KC .. t-1: in the fold of step t
-                        const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
+                        const bool win = lac != NC_NEVER && C.t - lac >= 1 && C.t - lac <= C.kc;
                         const uint32_t wm = __ballot_sync(kFull, win);
-                        if (lane == 0 && c * 32 < nsyn) P.win[(sb >> 5) + c] = wm;
+                        if (lane == 0 && (h + u) * 32 < u_rem) win_u[h + u] = wm;
                         const uint32_t lm = __ballot_sync(kFull, launch);
                         if (lm) {
                             if (launch) {
                                 const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                                ws.qs[pos] = (int32_t)(s - s_span);
+                                ws.qs[pos] = qoff + q;
                                 ws.qx[pos] = x;
                             }
                             qn += __popc(lm);
                             if (qn >= 32) {
                                 __syncwarp();
-                                P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                                P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], C.e_term);
                                 __syncwarp();
                                 if (lane < qn - 32) {
                                     ws.qs[lane] = ws.qs[32 + lane];
@@ -550,7 +585,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
                 const bool more = half + 1 < kUnitsPerSpan && ((bits >> ((k + 1) % kStages)) & 1);
                 if (!more) {
                     __syncwarp();
-                    if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], D.e_term);
+                    if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], C.e_term);
                     qn = 0;
                     acc[0] += (unsigned long long)warp_sum(nl);
                     acc[1] += (unsigned long long)warp_sum(nd);
@@ -719,6 +754,9 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
             // AP (src/NeuCor.cpp:706-714)
             if (lf != NC_NEVER && t - lf < kc) pot = __ldg(P.tables + D.ap_base + (t - lf));
             P.pot[pj] = pot;
+            // the post state the next synapse pass reads: getTrace at t (src/NeuCor.cpp:671-675,
+            // 0 when it fired at t), its sign set when it fired at t
+            P.pst[pj] = fired ? -0.0f : trace_at(P.tables + D.table_base + D.tab_pre_len, D.tab_post_len, t, lf);
         }
         const uint32_t fmask = __ballot_sync(kFull, fired);
         if (lane == 0) {

@@ -134,6 +134,9 @@ struct NcPools {
     int32_t* csc_post;   // target's device slot (local to the net)
     uint16_t* csc_dl;    // delay | target-above-source << 14 | target-below-source << 15
     int32_t* la_c;       // arrival step of the last accepted launch
+    float* pst;          // per neuron, written by the neuron pass of step t for the synapse
+                         // pass of t+1: the postsynaptic trace at t (getTrace), or -0.0
+                         // when the neuron fired at t
     uint32_t* win;       // bit per synapse: arrived within the fold window of the net's step
     NcTile* spans;       // work items of the synapse pass
     int32_t n_spans;

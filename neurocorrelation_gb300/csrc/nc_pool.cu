@@ -190,6 +190,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         NC_ALLOC(P.csc_post, int32_t, syn);
         NC_ALLOC(P.csc_dl, uint16_t, syn);
         NC_ALLOC(P.la_c, int32_t, syn);
+        NC_ALLOC(P.pst, float, neurons);
         NC_ALLOC(P.win, uint32_t, syn / 32 + 1);
         NC_ALLOC(P.spans, NcTile, spans);
     } else {

@@ -236,6 +236,7 @@ int nc_server::init(std::string& err)
         S_AL(P.csc_post, int32_t, syn_cap);
         S_AL(P.csc_dl, uint16_t, syn_cap);
         S_AL(P.la_c, int32_t, syn_cap);
+        S_AL(P.pst, float, neuron_cap);
         S_AL(P.win, uint32_t, syn_cap / 32 + 1);
         S_AL(P.spans, NcTile, span_cap);
         S_AL(d_nspans, int32_t, 1);

@@ -293,7 +293,7 @@ def background_draws(seed: int, n: int, dt: float, counter: int):
 
 
 # ------------------------------------------------------------- Oracle-R runner
-MODES = {"canonical": 0, "native": 1, "continuous": 2, "continuous_grid": 3, "construct": 4}
+MODES = {"canonical": 0, "native": 1, "continuous": 2, "continuous_grid": 3, "construct": 4, "inputs": 5}
 
 
 def reference_available() -> bool:
@@ -301,7 +301,7 @@ def reference_available() -> bool:
 
 
 def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps=100, record_pot=False,
-                  extra_fires=(), checkpoints=(), firers=()):
+                  extra_fires=(), checkpoints=(), firers=(), detectors=()):
     """Run the reference's own simulator on a scenario.  extra_fires: (step, id) pairs
     requesting a forced fire at that step.  firers: the reference's periodic input
     firers as dicts (pos, radius, rate_hz, offset_ms), continuous mode only.
@@ -343,6 +343,9 @@ def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps
             for fr in firers:
                 x, y, z = fr["pos"]
                 f.write(struct.pack("<6f", x, y, z, fr["radius"], fr["rate_hz"], fr.get("offset_ms", 0.0)))
+            f.write(struct.pack("<i", len(detectors)))
+            for d in detectors:
+                f.write(struct.pack("<4f", *[float(v) for v in d]))
         subprocess.run([REF_BIN, scen, outp], check=True)
         data = open(outp, "rb").read()
     row = (n + 7) // 8
@@ -361,9 +364,20 @@ def run_reference(mode, xyz, pre, post, weight, params: Params, groups=(), steps
     off += s
     nf = len(firers)
     flast = np.frombuffer(data, dtype=np.float32, count=nf * steps, offset=off).reshape(steps, nf)
+    off += 4 * nf * steps
+    rec = np.dtype([("from_id", "<i4"), ("to_id", "<i4"), ("weight", "<f4"), ("pre_potential", "<f4"),
+                    ("post_potential", "<f4"), ("inhibitory", "u1")])
+    snaps = []
+    for _ in checkpoints:
+        c = struct.unpack_from("<q", data, off)[0]
+        off += 8
+        snaps.append(np.frombuffer(data, dtype=rec, count=c, offset=off).copy())
+        off += rec.itemsize * c
+    nd = len(detectors)
+    volts = np.frombuffer(data, dtype=np.float32, count=nd * len(checkpoints), offset=off).reshape(len(checkpoints), nd)
     return {"raster": raster.copy(), "pots": None if pots is None else pots.copy(), "weights": ckw.copy(),
             "pot": fin[:n].copy(), "activity": fin[n:2 * n].copy(), "last_fire": fin[2 * n:].copy(),
-            "inhibitory": inh.copy(), "firer_last": flast.copy()}
+            "inhibitory": inh.copy(), "firer_last": flast.copy(), "snapshots": snaps, "voltages": volts.copy()}
 
 
 def reference_construct(n: int, seed: int):
@@ -385,6 +399,7 @@ def reference_construct(n: int, seed: int):
             f.write(struct.pack("<i", 0))
             f.write(struct.pack("<i", 0))
             f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", 0))
         subprocess.run([REF_BIN, scen, outp], check=True)
         data = open(outp, "rb").read()
     s = struct.unpack_from("<q", data, 0)[0]
@@ -399,6 +414,36 @@ def reference_construct(n: int, seed: int):
     off += 4 * s
     ln = np.frombuffer(data, np.float32, s, off).copy()
     return xyz, fr, to, w, ln
+
+
+def reference_input_snapshots(xyz, rates, seed: int):
+    """srand(seed); NeuCor(0) with neurons at xyz; setInputRateArray(rates, n, NULL, NULL)
+    in the reference: its getInputSnapshots as (id, x, y, z, radius, frequency, enabled)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+    firers = [dict(pos=(0.0, 0.0, 0.0), radius=1.0, rate_hz=float(r)) for r in rates]
+    p = default_params(seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        scen = os.path.join(td, "s.bin")
+        outp = os.path.join(td, "o.bin")
+        with open(scen, "wb") as f:
+            f.write(b"NCRF")
+            f.write(struct.pack("<iiq", MODES["inputs"], xyz.shape[0], 0))
+            f.write(xyz.tobytes())
+            f.write(struct.pack("<6f", p.run_speed, p.learning_rate, p.presynaptic_trace_decay,
+                                p.postsynaptic_trace_decay, p.presynaptic_factor, p.postsynaptic_factor))
+            f.write(struct.pack("<iQ", p.background_firing, p.seed))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<ii", 0, 0))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", 0))
+            f.write(struct.pack("<i", len(firers)))
+            for fr in firers:
+                f.write(struct.pack("<6f", 0.0, 0.0, 0.0, 1.0, fr["rate_hz"], 0.0))
+            f.write(struct.pack("<i", 0))
+        subprocess.run([REF_BIN, scen, outp], check=True)
+        data = open(outp, "rb").read()
+    rec = np.dtype([("v", "<f4", 6), ("enabled", "u1")])
+    return np.frombuffer(data, dtype=rec)
 
 
 def unpack_raster(raster, n):

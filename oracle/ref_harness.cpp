@@ -29,6 +29,9 @@
 //   4 construct  — srand(seed); NeuCor(n) (NeuCor.cpp:17-42); writes the positions
 //                  and every synapse (source, target, weight, length) in the
 //                  reference's own order.
+//   5 inputs     — srand(seed); NeuCor(0) with the scenario's neurons; then
+//                  setInputRateArray(rates, count, NULL, NULL) (random firer
+//                  positions, NeuCor.cpp:46-64, 309-313); writes getInputSnapshots.
 // Modes 0, 1 and 3 set every synapse length to delay*dt/AP_speed so spikes arrive
 // on the step grid.
 #include "NeuCor.h"
@@ -86,6 +89,9 @@ struct Scenario {
     // periodic input firers (NeuCor::setInputRateArray, NeuCor.cpp:46-64), continuous mode only
     std::vector<coord3> firer_pos;
     std::vector<float> firer_radius, firer_rate, firer_offset;
+    // voltage detectors (NeuCor::setDetectors, NeuCor.cpp:70-77): position and radius
+    std::vector<coord3> det_pos;
+    std::vector<float> det_radius;
 };
 
 template <class T>
@@ -122,6 +128,13 @@ static Scenario read_scenario(const char* path)
         float v[6]; rd(f, v, 6);
         sc.firer_pos.push_back(coord3{v[0], v[1], v[2]});
         sc.firer_radius.push_back(v[3]); sc.firer_rate.push_back(v[4]); sc.firer_offset.push_back(v[5]);
+    }
+    int32_t nd = 0;
+    if (fread(&nd, sizeof(nd), 1, f) != 1) nd = 0;  // older scenario files end here
+    for (int32_t i = 0; i < nd; ++i) {
+        float v[4]; rd(f, v, 4);
+        sc.det_pos.push_back(coord3{v[0], v[1], v[2]});
+        sc.det_radius.push_back(v[3]);
     }
     fclose(f);
     return sc;
@@ -170,6 +183,9 @@ public:
             for (size_t i = 0; i < rates_.size(); ++i)
                 if (sc_.firer_offset[i] != 0.0f) brain_->addInputOffset((unsigned)i, sc_.firer_offset[i]);
         }
+        if (!sc_.det_radius.empty())
+            brain_->setDetectors((unsigned)sc_.det_radius.size(), const_cast<coord3*>(sc_.det_pos.data()),
+                                 const_cast<float*>(sc_.det_radius.data()));
         // scheduledFireTime is never initialised by the Neuron constructor
         // (NeuCor.cpp:368-395); give it a time that is never reached.
         for (auto& neu : brain_->neurons) neu.scheduleFire(1e30f);
@@ -181,6 +197,8 @@ public:
         std::vector<float> pots;
         if (sc_.record_pot) pots.resize((size_t)n * sc_.steps);
         std::vector<float> ckw;
+        std::vector<uint8_t> cks;   // synapse snapshots at the checkpoints (packed records)
+        std::vector<float> volts;   // detector voltages at the checkpoints
         std::vector<float> firer_last;  // InputFirer::lastFire of every firer after each run call
         std::vector<uint8_t> hit(n);
         std::vector<int32_t> target(n), ids(n > 0 ? n : 1);
@@ -232,6 +250,8 @@ public:
             }
             while (ck < sc_.checkpoints.size() && sc_.checkpoints[ck] == t) {
                 append_weights(ckw);
+                append_snapshots(cks);
+                for (float v : brain_->getDetectorVoltages()) volts.push_back(v);
                 ck++;
             }
         }
@@ -254,6 +274,9 @@ public:
         }
         fwrite(inh.data(), 1, inh.size(), out);
         fwrite(firer_last.data(), sizeof(float), firer_last.size(), out);
+        // NeuCor::getSynapseSnapshots at every checkpoint, then getDetectorVoltages
+        fwrite(cks.data(), 1, cks.size(), out);
+        fwrite(volts.data(), sizeof(float), volts.size(), out);
         fclose(out);
         delete brain_;
         return 0;
@@ -281,6 +304,25 @@ private:
                 if (hit[i]) brain_->neurons[target[i]].scheduleFire(dt);
         }
         request_inputs(t, dt, ids);
+    }
+
+    // Per checkpoint: int64 count, then count records of {int32 from, int32 to, float
+    // weight, float prePotential, float postPotential, uint8 inhibitory} (21 bytes).
+    void append_snapshots(std::vector<uint8_t>& out)
+    {
+        const auto snaps = brain_->getSynapseSnapshots();
+        const int64_t c = (int64_t)snaps.size();
+        const uint8_t* cp = (const uint8_t*)&c;
+        out.insert(out.end(), cp, cp + sizeof(c));
+        for (const auto& sn : snaps) {
+            const int32_t ids[2] = {(int32_t)sn.fromID, (int32_t)sn.toID};
+            const float v[3] = {sn.weight, sn.prePotential, sn.postPotential};
+            const uint8_t* a = (const uint8_t*)ids;
+            out.insert(out.end(), a, a + sizeof(ids));
+            const uint8_t* b = (const uint8_t*)v;
+            out.insert(out.end(), b, b + sizeof(v));
+            out.push_back(sn.inhibitory ? 1 : 0);
+        }
     }
 
     void append_weights(std::vector<float>& out)
@@ -330,6 +372,25 @@ static int construct(const Scenario& sc, const char* out_path)
     return 0;
 }
 
+static int inputs(const Scenario& sc, const char* out_path)
+{
+    srand((unsigned)sc.p.seed);
+    NeuCor brain(0);
+    for (int32_t i = 0; i < sc.n; ++i) brain.createNeuron(coord3{sc.xyz[3 * i], sc.xyz[3 * i + 1], sc.xyz[3 * i + 2]});
+    std::vector<float> rates = sc.firer_rate;  // borrowed by the brain, as in NeuCor
+    brain.setInputRateArray(rates.data(), (unsigned)rates.size(), nullptr, nullptr);
+    FILE* out = fopen(out_path, "wb");
+    if (!out) { perror(out_path); return 2; }
+    for (const auto& s : brain.getInputSnapshots()) {
+        const float v[6] = {(float)s.id, s.position.x, s.position.y, s.position.z, s.radius, s.frequency};
+        fwrite(v, sizeof(float), 6, out);
+        const uint8_t en = s.enabled ? 1 : 0;
+        fwrite(&en, 1, 1, out);
+    }
+    fclose(out);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc != 3) {
@@ -338,6 +399,7 @@ int main(int argc, char** argv)
     }
     Scenario sc = read_scenario(argv[1]);
     if (sc.mode == 4) return construct(sc, argv[2]);
+    if (sc.mode == 5) return inputs(sc, argv[2]);
     srand((unsigned)sc.p.seed);
     NeuCor_Renderer drv(sc);
     return drv.run(argv[2]);

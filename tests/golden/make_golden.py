@@ -5,7 +5,7 @@ its sources by oracle/Makefile — on small seeded scenarios and stores inputs a
 outputs.  Needs the reference tree (this script does not run on the GPU machines;
 its outputs are committed).
 
-    python tests/golden/make_golden.py [base] [c1_stats]
+    python tests/golden/make_golden.py [base] [c1_stats] [snapshots]
 """
 import os
 import sys
@@ -88,12 +88,59 @@ def c1_statistics():
     save("c1_reference_stats", seeds=np.asarray(C1_SEEDS), steps=np.asarray(10000), window=np.asarray(1000), **out)
 
 
+def snapshots():
+    """G. The renderer's read-backs through the reference's own code at checkpoints:
+    NeuCor::getSynapseSnapshots (weights and the pre/post render potentials of spikes in
+    flight, src/NeuCor.cpp:115-134, 547-570) and NeuCor::getDetectorVoltages
+    (src/NeuCor.cpp:79-87, 359-366), canonical step order, at dt 1 and dt 0.5."""
+    cases = [
+        ("snapshots_knn64", knn_net(64, 6, 11, inhibitory=0.2), O.default_params(seed=5),
+         [dict(first=0, count=8, rate_hz=40.0, correlated=1, jitter=2)], 120, [1, 2, 3, 17, 60, 119, 120]),
+        ("snapshots_random40_dt05", random_net(40, 300, 3), O.default_params(seed=9, run_speed=0.5),
+         [dict(first=0, count=6, rate_hz=60.0, correlated=1, jitter=3)], 90, [4, 5, 31, 90]),
+        ("snapshots_knn200_busy", knn_net(200, 20, 13), O.default_params(seed=21),
+         [dict(first=0, count=20, rate_hz=40.0, correlated=1, jitter=2)], 60, [10, 11, 12, 40, 60]),
+    ]
+    for name, net, params, groups, steps, ck in cases:
+        xyz, pre, post, w = net
+        lo, hi = xyz.min(0), xyz.max(0)
+        det = [(float(lo[0] + (hi[0] - lo[0]) * f), float(lo[1] + (hi[1] - lo[1]) * f), float(lo[2] + (hi[2] - lo[2]) * f),
+                r) for f, r in [(0.5, 1.0), (0.25, 0.7), (0.8, 1.6)]]
+        r = O.run_reference("canonical", xyz, pre, post, w, params, groups=groups, steps=steps, checkpoints=ck,
+                            detectors=det)
+        sn = np.stack([np.stack([s[f].astype(np.float64) for f in ("from_id", "to_id", "weight", "pre_potential",
+                                                                   "post_potential", "inhibitory")], 1)
+                       for s in r["snapshots"]])
+        save(name, xyz=xyz, pre=pre, post=post, w=w, groups=groups_arr(groups), steps=np.asarray(steps),
+             checkpoints=np.asarray(ck, np.int32), detectors=np.asarray(det, np.float32),
+             snap_from=sn[:, :, 0].astype(np.int32), snap_to=sn[:, :, 1].astype(np.int32),
+             snap_weight=sn[:, :, 2].astype(np.float32), snap_pre=sn[:, :, 3].astype(np.float32),
+             snap_post=sn[:, :, 4].astype(np.float32), snap_inh=sn[:, :, 5].astype(np.uint8),
+             voltages=r["voltages"], **{"p_" + k: v for k, v in params_dict(params).items()})
+        nz = int((sn[:, :, 3] != 0).sum())
+        print(name, "spikes in flight over the checkpoints:", nz)
+
+
+def input_snapshots():
+    """H. NeuCor::getInputSnapshots after srand(4); NeuCor(0); 30 neurons;
+    setInputRateArray(rates, 5, NULL, NULL): firer positions drawn from the C library's
+    rand() in the reference's order (src/NeuCor.cpp:46-64, 309-313)."""
+    xyz = (np.random.default_rng(8).random((30, 3)) * 3.0 - 1.5).astype(np.float32)
+    rates = np.array([20.0, 0.0, 55.5, 13.0, 100.0], np.float32)
+    r = O.reference_input_snapshots(xyz, rates, 4)
+    save("input_snapshots_seed4", xyz=xyz, rates=rates, seed=np.asarray(4), snap=r["v"].copy(),
+         enabled=r["enabled"].copy())
+
+
 def main(sections):
     if not O.reference_available():
         O.build()
     assert O.reference_available(), "needs the reference tree to build oracle/_ref"
     if "c1_stats" in sections:
         c1_statistics()
+    if "snapshots" in sections:
+        snapshots()
+        input_snapshots()
     if "base" not in sections:
         return
 
@@ -156,4 +203,4 @@ def main(sections):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["base", "c1_stats"])
+    main(sys.argv[1:] or ["base", "c1_stats", "snapshots"])
