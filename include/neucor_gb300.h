@@ -312,7 +312,11 @@ typedef struct {
     int32_t launch_block;        /* event form: threads per block of the spike launch (32..256) */
     int32_t graph_steps;         /* steps per captured CUDA graph */
     int32_t dense_blocks;        /* dense form: blocks of the synapse pass (a grid-stride loop over
-                                    256-synapse spans); 0 = 4 per SM */
+                                    256-synapse spans); 0 = one wave of resident blocks */
+    int32_t steps_per_launch;    /* dense form: 0 = each step is two launches (replayed through CUDA
+                                    graphs of graph_steps steps); k > 0 = k whole steps per
+                                    persistent cooperative launch (grid barriers between the
+                                    passes; networks with periodic input firers use graphs) */
 } nc_launch_config;
 
 int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out);
@@ -325,9 +329,11 @@ int nc_batch_time(nc_batch* batch, int32_t steps, float* ms);
 int nc_batch_run_to_end(nc_batch* batch);
 int nc_batch_get_launch(nc_batch* batch, nc_launch_config* out);
 int nc_batch_set_launch(nc_batch* batch, const nc_launch_config* cfg);
-/* Times `steps_per_trial` steps under each candidate configuration (the simulation
- * advances during the trials; results do not depend on the configuration) and keeps
- * the fastest; *best receives it. */
+/* Times `steps_per_trial` steps under each candidate configuration, three times each
+ * after a warm-up trial, and keeps the one with the lowest median; *best receives it.
+ * The candidates cover block sizes, the synapse pass's grid, graph length and (dense
+ * form) steps per persistent launch.  The simulation advances during the trials; the
+ * results do not depend on the configuration. */
 int nc_batch_autotune(nc_batch* batch, int32_t steps_per_trial, nc_launch_config* best);
 int nc_batch_get_stats(nc_batch* batch, int32_t net, nc_stats* out);
 int nc_batch_get_step(nc_batch* batch, int32_t net, int64_t* step);

@@ -81,7 +81,8 @@ class NetSpec(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("neuron_block", ctypes.c_int32), ("launch_blocks", ctypes.c_int32), ("launch_block", ctypes.c_int32),
-                ("graph_steps", ctypes.c_int32), ("dense_blocks", ctypes.c_int32)]
+                ("graph_steps", ctypes.c_int32), ("dense_blocks", ctypes.c_int32),
+                ("steps_per_launch", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}

@@ -35,6 +35,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 namespace {
@@ -42,18 +43,7 @@ namespace {
 using namespace nc_dev;
 
 constexpr int kMaxWarps = 8;  // 256 threads per block at most
-
-#ifndef NC_DENSE_UNROLL
-#define NC_DENSE_UNROLL 2
-#endif
-constexpr int kUnroll = NC_DENSE_UNROLL;  // chunks whose loads are in flight together
-constexpr int kQueue = 64;                // launched-term queue per warp
-static_assert(NC_SPAN_CHUNKS % kUnroll == 0, "span chunks must be a multiple of the unroll");
-
-struct SynShared {
-    int32_t qs[kMaxWarps][kQueue];  // launched synapse, relative to its span's first
-    float qx[kMaxWarps][kQueue];    // deltaT * AP_depolFac of the launch
-};
+constexpr int kQueue = 64;    // launched-term queue per warp
 
 // Programmatic dependent launch: each pass of the dense step is launched so that its
 // blocks may be scheduled while the previous pass drains, and waits here, before it
@@ -74,131 +64,10 @@ __device__ __forceinline__ int warp_sum(int v)
     return v;
 }
 
-// deltaT*AP_depolFac*0.9943*exp(0.3702*deltaT) for the queued launches [0, count)
-// (src/NeuCor.cpp:695); lane l takes entry l.
-__device__ __forceinline__ void drain_terms(double* term_span, double e_term, SynShared& sh, int wib, int lane,
-                                            int count)
-{
-    __syncwarp();
-    if (lane < count) term_span[sh.qs[wib][lane]] = make_term(sh.qx[wib][lane], e_term);
-    __syncwarp();
-}
-
-// Synapse::fire and the deferred plasticity of step `prev` for the span's chunks (see
-// k_dense_synapses_direct); kAll: every chunk of the span lies inside the net.
-template <bool kAll>
-__device__ __forceinline__ void span_chunks(const NcPools& P, const NcNetDesc& D, SynShared& sh, int wib, int lane,
-                                            int64_t s_span, int32_t rem, int32_t t, int32_t prev, int& qn, int& nl,
-                                            int& nd)
-{
-    const int32_t kc = D.kc;
-    const uint32_t* fprev = P.fired + (int64_t)(prev & 1) * P.total_words + D.word_base;
-    const int32_t* lfn = P.lf + D.neuron_base;
-    const float* tab_pre = P.tables + D.table_base;
-    const float* tab_post = tab_pre + D.tab_pre_len;
-    // this lane's synapse in the span's first chunk, in every stream
-    const int32_t* pre_p = P.csc_pre + s_span + lane;
-    const int32_t* post_p = P.csc_post + s_span + lane;
-    const uint16_t* dl_p = P.csc_dl + s_span + lane;
-    int32_t* la_p = P.la_c + s_span + lane;
-    float* w_p = P.w + s_span + lane;
-    int32_t* ta_p = P.t_arr + s_span + lane;
-    const uint32_t* inh_p = P.inh + (s_span >> 5);
-    uint32_t* win_p = P.win + (s_span >> 5);
-    double* term_span = P.term + s_span;
-    const float dt = D.dt, c52 = D.c52;
-    for (int h = 0; h < NC_SPAN_CHUNKS; h += kUnroll) {
-        int32_t pre[kUnroll], post[kUnroll], la[kUnroll], ta[kUnroll], lfp[kUnroll];
-        uint32_t dl[kUnroll], fword[kUnroll], ihw[kUnroll];
-        float wv[kUnroll];
-        bool in[kUnroll];
-        // every load of the pass is issued before the first use
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const int q = (h + u) * 32;
-            in[u] = kAll || q < rem;
-            if (in[u]) {
-                pre[u] = __ldg(pre_p + q);
-                post[u] = __ldg(post_p + q);
-                dl[u] = __ldg(dl_p + q);
-                la[u] = la_p[q];
-                wv[u] = w_p[q];
-                ta[u] = ta_p[q];
-                ihw[u] = __ldg(inh_p + h + u);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            if (in[u]) {
-                fword[u] = fprev[pre[u] >> 5];
-                lfp[u] = lfn[post[u]];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const int q = (h + u) * 32;
-            int32_t lac = NC_NEVER;
-            bool launch = false;
-            float x = 0.0f;
-            if (in[u]) {
-                lac = la[u];
-                const bool tf = lfp[u] == prev;  // target fired at prev
-                const bool srcf = (fword[u] >> (pre[u] & 31)) & 1u;
-                const bool arrived = la[u] == prev;
-                const int32_t after = (int32_t)((dl[u] >> 14) & 1u);
-                launch = srcf && (la[u] == NC_NEVER || prev - la[u] >= kc + after);
-                nl += launch;
-                nd += srcf && !launch;
-                const bool ih = (ihw[u] >> lane) & 1u;
-                const float w0 = wv[u];
-                float w1 = w0;
-                if (tf) w1 = plasticity(w0, ih, trace_at(tab_pre, D.tab_pre_len, prev, ta[u]), 0.0f, D);
-                if (launch) {
-                    // target below the source in caller order and fired at prev: its
-                    // update ran first, post-spike plasticity included
-                    const float cap = (((dl[u] >> 15) & 1u) && tf) ? w1 : w0;
-                    // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                    x = dt * (c52 * cap);
-                    lac = prev + (int32_t)(dl[u] & 0x3fffu);
-                    la_p[q] = lac;
-                }
-                float w2 = w1;
-                if (arrived) {
-                    w2 = plasticity(w1, ih, 0.0f, trace_at(tab_post, D.tab_post_len, prev, lfp[u]), D);
-                    ta_p[q] = prev;
-                }
-                if (tf || arrived) w_p[q] = w2;
-            }
-            // arrived t-KC .. t-1: in the fold of step t
-            const bool win = lac != NC_NEVER && t - lac >= 1 && t - lac <= kc;
-            const uint32_t wm = __ballot_sync(kFull, win);
-            if (lane == 0 && (kAll || q < rem + lane)) win_p[h + u] = wm;
-            const uint32_t lm = __ballot_sync(kFull, launch);
-            if (lm) {
-                if (launch) {
-                    const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                    sh.qs[wib][pos] = q + lane;
-                    sh.qx[wib][pos] = x;
-                }
-                qn += __popc(lm);
-                if (qn >= 32) {
-                    drain_terms(term_span, D.e_term, sh, wib, lane, 32);
-                    if (lane < qn - 32) {
-                        sh.qs[wib][lane] = sh.qs[wib][32 + lane];
-                        sh.qx[wib][lane] = sh.qx[wib][32 + lane];
-                    }
-                    __syncwarp();
-                    qn -= 32;
-                }
-            }
-        }
-    }
-}
-
 // Adds each warp's per-net counters (K of them, into stats[first ..]) to the nets'
 // stats, summed per net over the block first.
 template <int K>
-__device__ void block_counters(const NcPools& P, int* s_net, unsigned long long (*s_acc)[K], int wib, int lane,
+__device__ void block_counters(const NcPools& P, int* s_net, unsigned long long (*s_acc)[2], int wib, int lane,
                                int acc_net, const unsigned long long* acc, int first)
 {
     if (lane == 0) {
@@ -227,54 +96,6 @@ __device__ void block_counters(const NcPools& P, int* s_net, unsigned long long 
                 if (tot[k]) atomicAdd(st + first + k, tot[k]);
         }
     }
-}
-
-template <bool kFlush>
-__global__ void __launch_bounds__(256, NC_DENSE_MIN_BLOCKS) k_dense_synapses_direct(NcPools P)
-{
-    __shared__ SynShared sh;
-    __shared__ int s_net[kMaxWarps];
-    __shared__ unsigned long long s_acc[kMaxWarps][2];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    wait_previous_pass();
-    const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
-
-    int acc_net = -1;
-    unsigned long long acc[2] = {0, 0};  // launched, dropped
-    for (int sp = gw; sp < n_spans; sp += nw) {
-        const NcTile span = P.spans[sp];
-        const NcNetDesc& D = P.nets[span.net];
-        const int32_t t = D.t;
-        const int32_t prev = t - 1;
-        // a flushed step finds its synapse pass done and its window bitmap written; a
-        // net's first step has nothing in flight (the bitmap starts cleared)
-        if (!D.active || prev < 1 || D.stdp_done >= prev) continue;
-        if (!kFlush && t > D.t_end) continue;
-        if (span.net != acc_net) {
-            if (acc_net >= 0 && lane == 0) {
-                unsigned long long* st = P.nets[acc_net].stats;
-                atomicAdd(st + 1, acc[0]);
-                atomicAdd(st + 2, acc[1]);
-            }
-            acc_net = span.net;
-            acc[0] = acc[1] = 0;
-        }
-        const int64_t s_span = D.syn_base + (int64_t)span.first * 32;
-        // synapses of the span inside the net, counted from this lane's first one
-        const int64_t rem64 = D.n_syn - (int64_t)span.first * 32 - lane;
-        int qn = 0, nl = 0, nd = 0;
-        if (D.n_syn - (int64_t)span.first * 32 >= NC_SPAN_CHUNKS * 32)
-            span_chunks<true>(P, D, sh, wib, lane, s_span, 0, t, prev, qn, nl, nd);
-        else
-            span_chunks<false>(P, D, sh, wib, lane, s_span, (int32_t)rem64, t, prev, qn, nl, nd);
-        if (qn > 0) drain_terms(P.term + s_span, D.e_term, sh, wib, lane, qn);
-        acc[0] += (unsigned long long)warp_sum(nl);
-        acc[1] += (unsigned long long)warp_sum(nd);
-    }
-    block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
 }
 
 // ---------------------------------------------------------------- staged synapse pass
@@ -390,25 +211,38 @@ __device__ __forceinline__ bool stage_wait(unsigned long long* bar, uint32_t pha
     return false;
 }
 
-template <bool kFlush>
-__global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools P)
-{
-    extern __shared__ __align__(128) unsigned char dyn_smem[];
-    __shared__ int s_net[kStageWarps];
-    __shared__ unsigned long long s_acc[kStageWarps][2];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kStageWarps + wib;
-    const int nw = gridDim.x * kStageWarps;
-    WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[wib];
+// The block's shared memory besides the stage buffers, used by both passes.
+struct PassShared {
+    int s_net[kMaxWarps];
+    unsigned long long s_acc[kMaxWarps][2];
+    int s_last;
+    int s_ok;
+    int s_cnt[kMaxWarps];
+    uint16_t s_list[kMaxWarps * 32];
+    float s_pot[kMaxWarps * 32];
+};
 
+// Lane 0 initialises the warp's stage barriers (once per launch).
+__device__ __forceinline__ void init_stages(WarpStage& ws, int lane)
+{
     if (lane == 0) {
         for (int k = 0; k < kStages; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&ws.bar[k])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
-    wait_previous_pass();
+}
+
+// The synapse pass of every span (see k_dense_synapses), each warp striding over the
+// grid's spans.  phases: the parity of each stage slot's next completion, carried from
+// one pass to the next within a launch.  All threads of the block call it.
+template <bool kFlush>
+__device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, PassShared& sh, uint32_t& phases)
+{
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kStageWarps + wib;
+    const int nw = gridDim.x * kStageWarps;
     const int n_spans = P.n_spans_dev ? *P.n_spans_dev : P.n_spans;
 
     // unit k of this warp: half k % kUnitsPerSpan of span gw + (k / kUnitsPerSpan) * nw,
@@ -422,7 +256,6 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
 
     int acc_net = -1, cur_net = -1;
     unsigned long long acc[2] = {0, 0};  // launched, dropped
-    uint32_t phases = 0u;  // bit j: parity of slot j's next completion
     bool ok = true;
     int qn = 0, nl = 0, nd = 0;
     for (int i = 0;; ++i) {
@@ -606,7 +439,23 @@ __global__ void __launch_bounds__(32 * kStageWarps, 3) k_dense_synapses(NcPools 
         for (int j = 0; j < kStages; ++j)
             if ((bits >> j) & 1) stage_wait(&ws.bar[j], (phases >> j) & 1u);
     }
-    block_counters<2>(P, s_net, s_acc, wib, lane, acc_net, acc, 1);
+    block_counters<2>(P, sh.s_net, sh.s_acc, wib, lane, acc_net, acc, 1);
+}
+
+#ifndef NC_STAGE_MIN_BLOCKS
+#define NC_STAGE_MIN_BLOCKS 4
+#endif
+
+template <bool kFlush>
+__global__ void __launch_bounds__(32 * kStageWarps, NC_STAGE_MIN_BLOCKS) k_dense_synapses(NcPools P)
+{
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    __shared__ PassShared sh;
+    WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[threadIdx.x >> 5];
+    init_stages(ws, threadIdx.x & 31);
+    wait_previous_pass();
+    uint32_t phases = 0u;  // bit j: parity of slot j's next completion
+    synapse_pass<kFlush>(P, ws, sh, phases);
 }
 
 // charge_insynapses (src/NeuCor.cpp:688-700) of neuron j of net D: the terms of the
@@ -667,18 +516,24 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
 // folds are packed onto its first threads before they run: a warp's FP64 add costs the
 // same however few lanes are active, and at saturation two neurons in three are in
 // their AP.
-__global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcPools P)
+#ifndef NC_DNEURON_MAXT
+#define NC_DNEURON_MAXT 256
+#endif
+#ifndef NC_DNEURON_MINB
+#define NC_DNEURON_MINB NC_NEURON_MIN_BLOCKS
+#endif
+// The neuron pass of every tile (see k_dense_neurons), each block striding over groups
+// of tiles; the last block to finish advances the nets' step counters.  All threads of
+// the block call it.
+__device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
 {
-    __shared__ int s_net[kMaxWarps];
-    __shared__ unsigned long long s_acc[kMaxWarps][1];
-    __shared__ int s_last;
-    __shared__ int s_cnt[kMaxWarps];
-    __shared__ uint16_t s_list[kMaxWarps * 32];
-    __shared__ float s_pot[kMaxWarps * 32];
+    int* s_net = sh.s_net;
+    int* s_cnt = sh.s_cnt;
+    uint16_t* s_list = sh.s_list;
+    float* s_pot = sh.s_pot;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
-    wait_previous_pass();
     const int n_tiles = P.n_tiles_dev ? *P.n_tiles_dev : P.n_tiles;
 
     int acc_net = -1;
@@ -779,13 +634,13 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
             }
         }
     }
-    block_counters<1>(P, s_net, s_acc, wib, lane, acc_net, acc, 0);
+    block_counters<1>(P, s_net, sh.s_acc, wib, lane, acc_net, acc, 0);
     // the last block to finish advances the step counters
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(P.done_ctr, 1u) == gridDim.x - 1u);
+    if (threadIdx.x == 0) sh.s_last = (atomicAdd(P.done_ctr, 1u) == gridDim.x - 1u);
     __syncthreads();
-    if (s_last) {
+    if (sh.s_last) {
         __threadfence();
         for (int n = threadIdx.x; n < P.n_nets; n += blockDim.x) {
             NcNetDesc* D = P.nets + n;
@@ -800,6 +655,77 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_dense_neurons(NcP
     }
 }
 
+__global__ void __launch_bounds__(NC_DNEURON_MAXT, NC_DNEURON_MINB) k_dense_neurons(NcPools P)
+{
+    __shared__ PassShared sh;
+    wait_previous_pass();
+    neuron_pass(P, sh);
+}
+
+// ---------------------------------------------------------------- fused multi-step launch
+// `ticks` whole steps of every net in one cooperative launch: synapse pass, grid
+// barrier, neuron pass (whose last block advances the step counters), grid barrier.
+// The grid is at most one wave (cudaLaunchCooperativeKernel refuses more), so every
+// block reaches every barrier; each barrier wait is still bounded, and one that gives
+// up sets NC_DEV_ERR_BARRIER and ends its block.  It saves the per-step launches and
+// their drain and fill for batches of small networks.  (No periodic input firers: they
+// run as their own kernel before a step.)
+constexpr uint32_t kBarrierPolls = 1u << 24;  // polls (64 ns sleeps) before a barrier gives up
+
+// bar[0]: arrivals, bar[1]: generation.  gen: this block's view of the generation.
+__device__ bool grid_barrier(unsigned* bar, unsigned& gen, uint32_t* dev_err, PassShared& sh)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned g = gen;
+        if (atomicAdd(&bar[0], 1u) == gridDim.x - 1u) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicExch(&bar[1], g + 1u);
+        } else {
+            uint32_t it = 0;
+            while (atomicAdd(&bar[1], 0u) == g) {
+                if (++it > kBarrierPolls) {
+                    atomicOr(dev_err, NC_DEV_ERR_BARRIER);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        gen = g + 1u;
+        sh.s_ok = ok;
+    }
+    __syncthreads();
+    return sh.s_ok != 0;
+}
+
+#ifndef NC_FUSED_MIN_BLOCKS
+#define NC_FUSED_MIN_BLOCKS 3  // the neuron pass needs ~80 registers
+#endif
+__global__ void __launch_bounds__(32 * kStageWarps, NC_FUSED_MIN_BLOCKS) k_dense_fused(NcPools P, int32_t ticks,
+                                                                                     unsigned* bar)
+{
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    __shared__ PassShared sh;
+    WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[threadIdx.x >> 5];
+    init_stages(ws, threadIdx.x & 31);
+    unsigned gen = 0u;
+    if (threadIdx.x == 0) gen = atomicAdd(&bar[1], 0u);
+    uint32_t phases = 0u;
+    for (int32_t k = 0; k < ticks; ++k) {
+        synapse_pass<false>(P, ws, sh, phases);
+        if (!grid_barrier(bar, gen, P.dev_err, sh)) return;
+        neuron_pass(P, sh);
+        if (!grid_barrier(bar, gen, P.dev_err, sh)) return;
+        // the next pass's bulk copies read what other blocks stored in this launch
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+}
+
 // After a flush: the synapse pass of every active net's last step is done.
 __global__ void k_dense_mark_flushed(NcPools P)
 {
@@ -809,18 +735,13 @@ __global__ void k_dense_mark_flushed(NcPools P)
     }
 }
 
-// The staged synapse pass (bulk copies into shared memory) is the default; the
-// register-load form measured 5% slower on the persistent grid.
-#ifndef NC_DENSE_STAGED
-#define NC_DENSE_STAGED 1
-#endif
-
 // The synapse pass's grid: the launch configuration's, else a persistent grid of as
 // many blocks as fit on the GPU at once (one wave; each warp strides over many spans,
-// and the staged form keeps its next units' copies in flight meanwhile).  A grid of
-// one span per warp measured 12% (register form) to 25% (staged form) slower.
+// and keeps its next units' copies in flight meanwhile).  A grid of one span per warp
+// measured 25% slower.  (A form of the pass on register loads instead of bulk copies
+// measured 5% slower and was dropped.)
 struct SynKernel {
-    void (*fn)(NcPools);
+    const void* fn;
     int threads;
     size_t smem;
 };
@@ -828,22 +749,21 @@ struct SynKernel {
 template <bool kFlush>
 SynKernel syn_kernel()
 {
-    if (NC_DENSE_STAGED) return {k_dense_synapses<kFlush>, 32 * kStageWarps, kStageSmem};
-    return {k_dense_synapses_direct<kFlush>, 32 * kMaxWarps, 0};
+    return {(const void*)k_dense_synapses<kFlush>, 32 * kStageWarps, kStageSmem};
 }
 
-// Blocks of the persistent grid on the current device (cached per device; the staged
-// form's shared-memory opt-in is set here, before the first launch).  Returns 0 when
-// the device cannot run the pass (the launch then reports an error).
-template <bool kFlush>
-int resident_blocks()
+SynKernel fused_kernel() { return {(const void*)k_dense_fused, 32 * kStageWarps, kStageSmem}; }
+
+// Blocks of one wave of kernel k on the current device (cached per device and kernel;
+// the shared-memory opt-in is set here, before the first launch).  Returns 0 when the
+// device cannot run it (the launch then reports an error).
+int resident_blocks(const SynKernel& k, int which)
 {
-    static std::atomic<int> cache[64];
+    static std::atomic<int> cache[3][64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-    int n = cache[dev].load(std::memory_order_relaxed);
+    int n = cache[which][dev].load(std::memory_order_relaxed);
     if (n == 0) {
-        const SynKernel k = syn_kernel<kFlush>();
         if (k.smem > 48 * 1024 &&
             cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem) != cudaSuccess)
             return 0;
@@ -853,13 +773,19 @@ int resident_blocks()
             sms * per_sm <= 0)
             return 0;
         n = sms * per_sm;
-        cache[dev].store(n, std::memory_order_relaxed);
+        cache[which][dev].store(n, std::memory_order_relaxed);
     }
     return n;
 }
 
+template <bool kFlush>
+int resident_syn_blocks()
+{
+    return resident_blocks(syn_kernel<kFlush>(), kFlush ? 1 : 0);
+}
+
 // Launches fn<<<grid, block, smem, s>>>(P) as a programmatic dependent launch.
-cudaError_t launch_pdl(void (*fn)(NcPools), int grid, int block, size_t smem, cudaStream_t s, const NcPools& P)
+cudaError_t launch_pdl(const void* fn, int grid, int block, size_t smem, cudaStream_t s, const NcPools& P)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -871,7 +797,7 @@ cudaError_t launch_pdl(void (*fn)(NcPools), int grid, int block, size_t smem, cu
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = NC_PDL ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, fn, P);
+    return cudaLaunchKernelEx(&cfg, (void (*)(NcPools))fn, P);
 }
 
 template <bool kFlush>
@@ -881,7 +807,7 @@ int launch_syn(const NcPools& P, const nc::LaunchShape& L, cudaStream_t s)
     const int wpb = k.threads / 32;
     const int full = (P.n_spans + wpb - 1) / wpb;
     if (full <= 0) return 0;
-    const int resident = resident_blocks<kFlush>();
+    const int resident = resident_syn_blocks<kFlush>();
     if (resident <= 0) return -1;
     const int blocks = L.dense_blocks > 0 ? L.dense_blocks : (full < resident ? full : resident);
     return launch_pdl(k.fn, blocks, k.threads, k.smem, s, P) == cudaSuccess ? 0 : -1;
@@ -901,14 +827,38 @@ int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream)
 {
     const int wpb = L.neuron_block / 32;
     const int blocks = (P.n_tiles + wpb - 1) / wpb;
-    if (blocks > 0 && launch_pdl(k_dense_neurons, blocks, L.neuron_block, 0, (cudaStream_t)stream, P) != cudaSuccess)
+    if (blocks > 0 &&
+        launch_pdl((const void*)k_dense_neurons, blocks, L.neuron_block, 0, (cudaStream_t)stream, P) != cudaSuccess)
         return -1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int prepare_dense_launch()
 {
-    return resident_blocks<false>() > 0 && resident_blocks<true>() > 0 ? 0 : -1;
+    return resident_syn_blocks<false>() > 0 && resident_syn_blocks<true>() > 0 &&
+                   resident_blocks(fused_kernel(), 2) > 0
+               ? 0
+               : -1;
+}
+
+int launch_fused_dense(const NcPools& P, int32_t ticks, unsigned* bar, void* stream)
+{
+    if (ticks <= 0) return 0;
+    const int resident = resident_blocks(fused_kernel(), 2);
+    if (resident <= 0) return -1;
+    // as many blocks as the larger pass has work for, at most one wave: a barrier over
+    // fewer blocks is quicker
+    const int need = std::max((P.n_spans + kStageWarps - 1) / kStageWarps, (P.n_tiles + kStageWarps - 1) / kStageWarps);
+    const int blocks = std::max(1, std::min(resident, need));
+    const cudaStream_t s = (cudaStream_t)stream;
+    // the arrival count starts at zero (a barrier that gave up may have left it set)
+    if (cudaMemsetAsync(bar, 0, sizeof(unsigned), s) != cudaSuccess) return -1;
+    NcPools p = P;
+    void* args[] = {(void*)&p, (void*)&ticks, (void*)&bar};
+    if (cudaLaunchCooperativeKernel((const void*)k_dense_fused, dim3((unsigned)blocks), dim3(32 * kStageWarps),
+                                    args, kStageSmem, s) != cudaSuccess)
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream)

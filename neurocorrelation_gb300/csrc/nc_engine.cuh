@@ -37,6 +37,7 @@
 // Device error codes (NcPools::dev_err).
 #define NC_DEV_ERR_STAGE_TIMEOUT 1u  // a bulk copy into shared memory did not complete in time
 #define NC_DEV_ERR_FIRER_LOOP 2u     // an input firer's schedule did not advance (capped)
+#define NC_DEV_ERR_BARRIER 4u        // a grid barrier of the fused multi-step launch gave up
 
 // Draw streams (third Philox counter word).
 #define NC_STREAM_BACKGROUND 1u
@@ -212,6 +213,9 @@ namespace nc {
 #ifndef NC_DENSE_MIN_BLOCKS
 #define NC_DENSE_MIN_BLOCKS 4
 #endif
+#ifndef NC_DNEURON_BLOCK
+#define NC_DNEURON_BLOCK 128  // threads per block of the dense neuron pass
+#endif
 #ifndef NC_LAUNCH_MIN_BLOCKS
 #define NC_LAUNCH_MIN_BLOCKS 4
 #endif
@@ -221,6 +225,8 @@ struct LaunchShape {
     int launch_blocks;   // blocks of the spike-launch kernel
     int launch_block;    // threads per block of the spike-launch kernel
     int dense_blocks = 0; // blocks of the dense synapse pass (0: one warp per span)
+    int fused_ticks = 0;  // dense form: steps per fused cooperative launch (0: two launches
+                          // per step, replayed through CUDA graphs)
 };
 int launch_neuron_step(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_spike_launch(const NcPools& P, const LaunchShape& L, void* stream);
@@ -233,6 +239,9 @@ int launch_dense_neurons(const NcPools& P, const LaunchShape& L, void* stream);
 // the current device; called before a stream capture, where neither may happen.
 int prepare_dense_launch();
 int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
+// `ticks` whole dense steps of every net in one cooperative launch (no periodic input
+// firers); bar: two zero-initialised words of device memory for its grid barrier.
+int launch_fused_dense(const NcPools& P, int32_t ticks, unsigned* bar, void* stream);
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);

@@ -97,7 +97,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     dense = nets.empty() || nets[0]->p.step_mode == NC_STEP_DENSE;
     // the dense neuron pass is one wave: 128-thread blocks spread it more evenly over the
     // SMs (measured 2% faster on the 100k x 100 network than 256)
-    L.neuron_block = dense ? 128 : 256;
+    L.neuron_block = dense ? NC_DNEURON_BLOCK : 256;
     L.launch_block = 256;
     L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
 
@@ -217,6 +217,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_ALLOC(P.tick, int32_t, 1);
     NC_ALLOC(P.done_ctr, uint32_t, 1);
     NC_ALLOC(P.dev_err, uint32_t, 1);
+    NC_ALLOC(d_bar_, unsigned, 2);
     NC_ALLOC(d_stats_, unsigned long long, 4 * nets.size());
     P.n_nets = (int32_t)nets.size();
     P.n_tiles = (int32_t)tiles;
@@ -318,6 +319,18 @@ int Engine::capture_graph(std::string& err)
 int Engine::step(int64_t ticks, std::string& err)
 {
     if (ticks <= 0) return NC_OK;
+    if (dense && L.fused_ticks > 0 && P.n_firers == 0) {
+        // several whole steps per cooperative launch
+        while (ticks > 0) {
+            const int32_t m = (int32_t)std::min<int64_t>(ticks, L.fused_ticks);
+            if (launch_fused_dense(P, m, d_bar_, stream)) {
+                err = cuda_msg("fused step launch", cudaGetLastError());
+                return NC_ERR_CUDA;
+            }
+            ticks -= m;
+        }
+        return NC_OK;
+    }
     if (ticks >= graph_ticks && graph_ticks > 0) {
         if (!graph_) {
             const int rc = capture_graph(err);

@@ -83,6 +83,7 @@ private:
     int32_t* d_ids_ = nullptr;
     int ids_cap_ = 0;
     unsigned long long* d_stats_ = nullptr;
+    unsigned* d_bar_ = nullptr;  // grid barrier of the fused launch (arrivals, generation)
 };
 
 std::string cuda_msg(const char* what, cudaError_t e);

@@ -279,7 +279,7 @@ int nc_server::init(std::string& err)
     a_ring.reset(ring_cap);
     a_table.reset(table_cap);
     for (int32_t q = nets - 1; q >= 0; --q) free_slots.push_back(q);
-    L.neuron_block = dense ? 128 : 256;
+    L.neuron_block = dense ? NC_DNEURON_BLOCK : 256;
     L.launch_block = 256;
     L.launch_blocks = std::max(1, sms * NC_LAUNCH_MIN_BLOCKS);
     L.dense_blocks = 0;  // the synapse pass's persistent grid (its warps stride the span table)

@@ -62,14 +62,15 @@ def c1_workload():
 
 
 def c1_stats(mode, seed, steps=10000, window=1000):
-    """Population statistics of the reference's own NeuCor::run on the C1 workload."""
+    """Population statistics of the reference's own NeuCor::run on the C1 workload:
+    the population rate per 1,000-step window, per-neuron fire counts, and the final
+    weights (all excitatory, so in [0, 1]) quantised to 16 bits."""
     xyz, pre, post, w, groups = c1_workload()
-    ck = list(range(window, steps + 1, window))
     r = O.run_reference(mode, xyz, pre, post, w, O.default_params(seed=seed), groups=groups, steps=steps,
-                        checkpoints=ck)
+                        checkpoints=[steps])
     ras = O.unpack_raster(r["raster"], xyz.shape[0])
     pop = ras.reshape(steps // window, window, -1).sum((1, 2)) / (xyz.shape[0] * window / 1000.0)
-    wq = np.rint(np.clip(r["weights"], 0.0, 1.0) * 65535.0).astype(np.uint16)  # every 1,000 steps
+    wq = np.rint(np.clip(r["weights"][-1], 0.0, 1.0) * 65535.0).astype(np.uint16)
     return dict(pop_rate_hz=pop.astype(np.float64), counts=ras.sum(0).astype(np.int32), weights_u16=wq)
 
 
@@ -78,13 +79,16 @@ def c1_statistics():
     native: runAll, synapse lengths on the step grid (the benchmark spec's whole-step
     delays), background fire times on the step grid; three simulation seeds.
     continuous: the unmodified timing (lengths as built, glibc rand() background at
-    random times inside the step); one seed."""
+    random times inside the step); one seed.
+    continuous_grid: as continuous with the lengths on the step grid (only the
+    background fire times off it); one seed."""
+    import concurrent.futures as cf
+    runs = [("native", s) for s in C1_SEEDS] + [("continuous", C1_SEEDS[0]), ("continuous_grid", C1_SEEDS[0])]
     out = {}
-    for seed in C1_SEEDS:
-        for k, v in c1_stats("native", seed).items():
-            out[f"native_{seed}_{k}"] = v
-    for k, v in c1_stats("continuous", C1_SEEDS[0]).items():
-        out[f"continuous_{C1_SEEDS[0]}_{k}"] = v
+    with cf.ThreadPoolExecutor(len(runs)) as ex:  # each run is its own reference process
+        for (mode, seed), res in zip(runs, ex.map(lambda ms: c1_stats(*ms), runs)):
+            for k, v in res.items():
+                out[f"{mode}_{seed}_{k}"] = v
     save("c1_reference_stats", seeds=np.asarray(C1_SEEDS), steps=np.asarray(10000), window=np.asarray(1000), **out)
 
 

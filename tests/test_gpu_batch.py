@@ -61,9 +61,14 @@ def test_batch_each_net_as_alone(nc, oracle_mod, mode):
 def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod, mode):
     specs = mixed_nets()
     b = batch_of(nc, specs, mode)
-    shapes = [dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=0, dense_blocks=0),
-              dict(neuron_block=256, launch_blocks=1216, launch_block=256, graph_steps=7, dense_blocks=3),
-              dict(neuron_block=64, launch_blocks=3, launch_block=32, graph_steps=16, dense_blocks=304)]
+    shapes = [dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=0, dense_blocks=0,
+                   steps_per_launch=0),
+              dict(neuron_block=256, launch_blocks=1216, launch_block=256, graph_steps=7, dense_blocks=3,
+                   steps_per_launch=5),
+              dict(neuron_block=64, launch_blocks=3, launch_block=32, graph_steps=16, dense_blocks=304,
+                   steps_per_launch=0),
+              dict(neuron_block=128, launch_blocks=152, launch_block=128, graph_steps=16, dense_blocks=0,
+                   steps_per_launch=64)]
     done = 0
     for k, sh in enumerate(shapes * 10):
         b.set_launch(**sh)
@@ -74,6 +79,20 @@ def test_batch_results_do_not_depend_on_launch_shape(nc, oracle_mod, mode):
     b.run_to_end()
     for q, s in enumerate(specs):
         check_equal(b, q, oracle_of(oracle_mod, s))
+
+
+def test_batch_persistent_launch_each_net_as_alone(nc, oracle_mod):
+    """Dense form, several whole steps per cooperative launch (grid barriers between the
+    passes): every network still equals the oracle, at every launch length."""
+    specs = mixed_nets()
+    for k in (1, 16, 400):
+        b = batch_of(nc, specs, "dense")
+        b.set_launch(steps_per_launch=k)
+        b.run_to_end()
+        for q, s in enumerate(specs):
+            assert b.step(q) == s["horizon"]
+            check_equal(b, q, oracle_of(oracle_mod, s))
+        b.close()
 
 
 def test_batch_rejects_oversized_blocks(nc):
@@ -90,7 +109,7 @@ def test_batch_autotune_keeps_results(nc, oracle_mod, mode):
     specs = mixed_nets()
     b = batch_of(nc, specs, mode)
     cfg = b.autotune(steps_per_trial=2)
-    assert cfg["neuron_block"] % 32 == 0 and cfg["launch_blocks"] > 0
+    assert cfg["neuron_block"] % 32 == 0 and cfg["launch_blocks"] > 0 and cfg["steps_per_launch"] >= 0
     b.run_to_end()
     for q, s in enumerate(specs):
         check_equal(b, q, oracle_of(oracle_mod, s))
