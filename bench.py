@@ -303,12 +303,16 @@ def one_at_a_time(G, nets, mode, arrivals=None):
     return events, busy, run_s, lat
 
 
-def measure_batched(G, n_nets, horizon, mode):
+def measure_batched(G, n_nets, horizon, mode, one_at_a_time_sample=None):
+    t_gen = time.perf_counter()
     nets = c3_nets(G, n_nets, horizon)
+    t_build = time.perf_counter()
     b = G.Batch([dict(xyz=d["xyz"], pre=d["pre"], post=d["post"], weight=d["weight"],
                       params=G.default_params(seed=d["seed"], step_mode=mode), groups=d["groups"],
                       horizon=d["horizon"]) for d in nets])
-    cfg = b.autotune(steps_per_trial=4)
+    t_tune = time.perf_counter()
+    cfg = b.autotune(steps_per_trial=8)
+    t_run = time.perf_counter()
     done = b.step(0)
     before = sum(b.stats(q)["launched"] for q in range(n_nets))
     ms = b.time(horizon - done)
@@ -316,13 +320,19 @@ def measure_batched(G, n_nets, horizon, mode):
     neurons = sum(int(d["xyz"].shape[0]) for d in nets)
     synapses = sum(int(d["pre"].shape[0]) for d in nets)
     b.close()
-    sub = nets[: min(len(nets), 16)]
+    t_one = time.perf_counter()
+    sub = nets if not one_at_a_time_sample else nets[:one_at_a_time_sample]
     ev1, busy1, run1, _ = one_at_a_time(G, sub, mode)
+    t_end = time.perf_counter()
     rate = events * 1000.0 / ms
-    return {"networks": n_nets, "neurons": neurons, "synapses": synapses, "steps": horizon,
+    return {"workload": f"{n_nets} networks, sizes log-uniform 1k-64k neurons, fan-out 20-200 nearest, "
+                        f"input rate 5-50 Hz, 1-8 correlated groups, {horizon} steps each",
+            "networks": n_nets, "neurons": neurons, "synapses": synapses, "steps": horizon,
             "timed_steps": horizon - done, "launch_config": cfg, "events_per_s": rate,
-            "one_at_a_time_sample": f"the first {len(sub)} networks of the same generator, each created, "
-                                    "run for its horizon and read back alone",
+            "wall_s": {"generate": t_build - t_gen, "create": t_tune - t_build, "autotune": t_run - t_tune,
+                       "run": t_one - t_run, "one_at_a_time": t_end - t_one},
+            "one_at_a_time_sample": f"{'all' if len(sub) == len(nets) else 'the first ' + str(len(sub))} of the "
+                                    "networks, each created, run for its horizon and read back alone",
             "one_at_a_time_events_per_s": ev1 / run1,
             "one_at_a_time_events_per_s_with_build": ev1 / busy1,
             "speedup_vs_one_at_a_time": rate / (ev1 / run1)}
@@ -350,7 +360,9 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
     events = sum(d["launched"] for d in ok)
     ev1, busy1, _, lat1 = one_at_a_time(G, reqs, mode, arrivals=[r["arrival"] for r in reqs])
     span1 = max(a + l for a, l in zip([r["arrival"] for r in reqs], lat1)) - reqs[0]["arrival"]
-    return {"requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
+    return {"workload": f"{n_req} requests, Poisson arrivals at 50/s, 500-200k neurons, fan-out 20-150, "
+                        f"horizons log-uniform 1k-100k steps x {horizon_scale}, 1-8 input groups each",
+            "requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
             "budget_gb": budget / 1e9, "events_per_s": events / span, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "peak_resident_networks": sst["peak_resident_networks"],
             "peak_resident_gb": sst["peak_resident_bytes"] / 1e9,
@@ -529,7 +541,8 @@ def run_ours(args):
     if world == 1 and args.large:
         line["large_network"] = measure_large(G, mode)
     if world == 1 and args.forms:
-        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, mode),
+        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, mode,
+                                                    args.batched_one_at_a_time),
                          "served": measure_served(G, args.served_requests, args.served_horizon_scale,
                                                   args.served_budget_gb * 1e9, mode)}
     print(json.dumps(line), flush=True)
@@ -552,9 +565,11 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the batched and served samples")
-    ap.add_argument("--batched-nets", type=int, default=64)
-    ap.add_argument("--batched-steps", type=int, default=2000)
-    ap.add_argument("--served-requests", type=int, default=32)
+    ap.add_argument("--batched-nets", type=int, default=256)
+    ap.add_argument("--batched-steps", type=int, default=1000)
+    ap.add_argument("--batched-one-at-a-time", type=int, default=0,
+                    help="networks of the batched mix timed one at a time (0 = all)")
+    ap.add_argument("--served-requests", type=int, default=200)
     ap.add_argument("--served-horizon-scale", type=float, default=0.1)
     ap.add_argument("--served-budget-gb", type=float, default=120.0)
     ap.add_argument("--sim-steps-per-step", type=int, default=SIM_STEPS_PER_STEP,
