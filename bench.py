@@ -34,7 +34,8 @@ SIM_STEPS_PER_STEP = 1000
 N_GROUPS, GROUP_SIZE = 10, 20
 METRIC = "synaptic events/s"
 UNIT = "events/s"
-STEP_MODES = {"dense": 0, "event": 1}
+STEP_MODES = {"dense": 0, "event": 1, "auto": 2}
+FORM_NAMES = {0: "dense", 1: "event"}
 REF_PREWARM_STEPS = 40
 
 
@@ -401,6 +402,28 @@ def measure_large(G, mode, sim_steps=100, timed=5):
     return out
 
 
+def measure_sparse(G, arrays, groups, seed, warm=2000, timed=2000):
+    """The same network with its weights scaled by 0.05: activity stays near the input
+    and background rates (a few Hz), the regime where the event form is the fast one.
+    Timed in each form and in the automatic choice."""
+    xyz, pre, post, w = arrays
+    ws = (w * np.float32(0.05)).astype(np.float32)
+    out = {"workload": "100k x 100 network as the headline, weights x 0.05 (quiet), "
+                       f"{timed} steps after {warm}"}
+    for label in ("auto", "dense", "event"):
+        net = G.NeuCor.from_arrays(xyz, pre, post, ws, params=G.default_params(seed=seed, step_mode=STEP_MODES[label]))
+        net.set_input_groups(groups)
+        net.run(warm)
+        st0 = net.stats()
+        ms, _ = net.time_steps(timed)
+        st1 = net.stats()
+        out[label] = {"form": FORM_NAMES[net.step_form], "us_per_sim_step": ms * 1e3 / timed,
+                      "events_per_s": (st1["launched"] - st0["launched"]) / (ms / 1e3),
+                      "mean_rate_hz": (st1["fires"] - st0["fires"]) / (N_NEURONS * timed / 1000.0)}
+        net.close()
+    return out
+
+
 def aggregate_over_ranks(pg, secs, e2e_secs, events, e2e_events):
     """The whole job's timing and work: the slowest rank's seconds (timed region and end
     to end) and the events of all ranks.  pg: torch.distributed, or None for one rank."""
@@ -496,7 +519,8 @@ def run_ours(args):
     neuron_steps = N_NEURONS * args.steps * S * world / secs
     peak, peak_kind = measured_peak()
     n_ms, l_ms = per
-    if args.step_mode == "dense":
+    form = FORM_NAMES[net.step_form]  # the form the timed steps ran in (auto: the one it chose)
+    if form == "dense":
         # the synapse pass moves the 14 bytes per synaptic event (index 4, delay 2,
         # weight read + write 8), the neuron pass the 16 per neuron
         kernels = {"k_dense_synapses": n_ms, "k_dense_neurons": l_ms}
@@ -524,12 +548,12 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(),
-        "stats": {"step_mode": args.step_mode, "neuron_steps_per_s": neuron_steps,
+        "stats": {"step_mode": args.step_mode, "form": form, "neuron_steps_per_s": neuron_steps,
                   "spikes_per_s": fires * world / secs,
                   "mean_rate_hz": fires / (N_NEURONS * args.steps * S / 1000.0),
                   "timed_steps": f"{args.warmup * S + 1}-{(args.warmup + args.steps) * S}",
                   "step_alg_gbs": step_alg},
-        "gpu_launches": (1 if args.step_mode == "dense" else 2) * args.steps * S,
+        "gpu_launches": 2 * args.steps * S,  # two kernels per simulation step in either form
         "clocks": clk.summary(),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -538,13 +562,19 @@ def run_ours(args):
         "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
     }
+    if world == 1 and not args.no_sparse:
+        line["sparse_variant"] = measure_sparse(G, arrays, groups, seed)
+    # the batched and served forms run one form for all their networks, and the device
+    # builder of the large network makes the dense form: the automatic choice resolves to
+    # the dense form there (these workloads saturate)
+    fixed = mode if mode != STEP_MODES["auto"] else STEP_MODES["dense"]
     if world == 1 and args.large:
-        line["large_network"] = measure_large(G, mode)
+        line["large_network"] = measure_large(G, fixed)
     if world == 1 and args.forms:
-        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, mode,
+        line["forms"] = {"batched": measure_batched(G, args.batched_nets, args.batched_steps, fixed,
                                                     args.batched_one_at_a_time),
                          "served": measure_served(G, args.served_requests, args.served_horizon_scale,
-                                                  args.served_budget_gb * 1e9, mode)}
+                                                  args.served_budget_gb * 1e9, fixed)}
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
@@ -560,8 +590,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the 2M x 200 network (built on the device, timed over a prefix)")
-    ap.add_argument("--step-mode", default="dense", choices=sorted(STEP_MODES),
-                    help="form of the step kernels (results are the same in both)")
+    ap.add_argument("--step-mode", default="auto", choices=sorted(STEP_MODES),
+                    help="form of the step kernels (results are the same in all); auto switches by activity")
+    ap.add_argument("--no-sparse", action="store_true",
+                    help="skip the quiet variant of the workload (weights x 0.05)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the batched and served samples")

@@ -85,9 +85,15 @@ typedef struct {
  *   NC_STEP_EVENT  two launches per step; fired neurons are compacted into a list and
  *                  only their out-synapses and the arrived spikes are touched.  Its cost
  *                  grows with the synaptic events: the faster form for sparse activity.
- * Networks batched into one engine (nc_batch_create) run in the first network's form. */
+ *   NC_STEP_AUTO   a single network (nc_create, nc_create_knn) holds the tables of both
+ *                  forms and switches between them at run-call boundaries from the share
+ *                  of neurons that fired in the last window of steps (see nc_run); the
+ *                  switch keeps every bit of the state.  It costs the memory of both forms.
+ * Networks batched into one engine (nc_batch_create) run in the first network's form
+ * (dense or event). */
 #define NC_STEP_DENSE 0
 #define NC_STEP_EVENT 1
+#define NC_STEP_AUTO 2
 
 /* A group of input neurons driven by Poisson spike trains.  Members are the
  * neurons first .. first+count-1.  Correlated groups share one source whose every
@@ -197,8 +203,22 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* neuron_ids);
 
 /* ------------------------------------------------------------------ run */
 /* Advances n_steps steps (NeuCor::run called n_steps times, src/NeuCor.cpp:583-617).
- * Asynchronous on the handle's stream; read-backs synchronise. */
+ * Asynchronous on the handle's stream; read-backs synchronise.  A network in
+ * NC_STEP_AUTO runs in windows of NC_AUTO_WINDOW steps and reads its fire count after
+ * each (a synchronisation): it moves to the event form when fewer than
+ * NC_AUTO_TO_EVENT_PERMILLE per mille of its neurons fired per step in the window, and
+ * back to the dense form above NC_AUTO_TO_DENSE_PERMILLE (the measured crossover of the
+ * two forms on a 100k-neuron, 100-fan-out network lies between). */
+#define NC_AUTO_WINDOW 256
+#define NC_AUTO_TO_EVENT_PERMILLE 100
+#define NC_AUTO_TO_DENSE_PERMILLE 160
 int nc_run(nc_net* net, int32_t n_steps);
+/* The form the network's next steps run in (NC_STEP_DENSE or NC_STEP_EVENT).  A network
+ * created with NC_STEP_AUTO may be switched by the caller with nc_set_step_form (form
+ * NC_STEP_DENSE or NC_STEP_EVENT pins it, NC_STEP_AUTO hands the choice back to nc_run);
+ * other networks accept only their own form.  No counterpart in the reference. */
+int nc_get_step_form(nc_net* net, int32_t* form);
+int nc_set_step_form(nc_net* net, int32_t form);
 /* Waits for the handle's queued work. */
 int nc_sync(nc_net* net);
 /* NeuCor::getTime (src/NeuCor.cpp:225): simulated ms, accumulated in float like the

@@ -25,6 +25,7 @@ _LIB = os.path.join(_HERE, "_lib", "libneucor_gb300.so")
 NC_OK = 0
 NC_STEP_DENSE = 0  # step_mode: one launch per step, in-rows walked in order
 NC_STEP_EVENT = 1  # step_mode: fired-list compaction and spike launch (sparse activity)
+NC_STEP_AUTO = 2   # step_mode: both forms' tables; nc_run switches by the fire share
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "no CUDA device",
            -6: "device wait timed out", -7: "over memory budget"}
 
@@ -119,6 +120,7 @@ def load_library() -> ctypes.CDLL:
         "nc_read_inhibitory": ([P, P], I32),
         "nc_read_synapse_snapshots": ([P, P, I64, P], I32), "nc_reset_activities": ([P], I32),
         "nc_read_input_snapshots": ([P, P, I32, P], I32),
+        "nc_get_step_form": ([P, P], I32), "nc_set_step_form": ([P, I32], I32),
         "nc_get_stats": ([P, P], I32), "nc_delete_synapse": ([P, I32, I32], I32),
         "nc_delete_neuron": ([P, I32], I32),
         "nc_build_knn": ([I32, I32, F, ctypes.c_uint64, P, P, P, P], I32),
@@ -478,6 +480,17 @@ class NeuCor:
 
     def sync(self):
         _check(self._lib.nc_sync(self._handle()))
+
+    @property
+    def step_form(self) -> int:
+        """The form the next steps run in: NC_STEP_DENSE or NC_STEP_EVENT."""
+        v = ctypes.c_int32()
+        _check(self._lib.nc_get_step_form(self._handle(), ctypes.byref(v)))
+        return int(v.value)
+
+    def set_step_form(self, form: int):
+        """Pin a network created with NC_STEP_AUTO to a form, or hand the choice back (NC_STEP_AUTO)."""
+        _check(self._lib.nc_set_step_form(self._handle(), int(form)))
 
     def getTime(self) -> float:
         v = ctypes.c_float()

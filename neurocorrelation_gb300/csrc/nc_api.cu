@@ -144,6 +144,7 @@ int nc_create(int32_t n_neurons, const float* xyz, int64_t n_synapses, const int
         delete net;
         return fail(rc, err);
     }
+    net->auto_form = params->step_mode == NC_STEP_AUTO;
     // keep on the host only what read-back needs (the out-synapse tables serve the
     // synapse snapshots)
     nc::NetHost& h = net->host;
@@ -436,14 +437,64 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* ids)
     return NC_OK;
 }
 
+// Steps the engine; a network in NC_STEP_AUTO runs window by window and, after each,
+// moves to the form its fire share calls for (NC_AUTO_* in neucor_gb300.h).
+static int advance(nc_net* net, int64_t n_steps)
+{
+    if (!net->auto_form) {
+        NC_CALL(net->eng, step, n_steps);
+        return NC_OK;
+    }
+    const int32_t n = std::max(net->host.n, 1);
+    while (n_steps > 0) {
+        const int64_t m = std::min<int64_t>(n_steps, NC_AUTO_WINDOW);
+        NC_CALL(net->eng, step, m);
+        unsigned long long st[4];
+        NC_CALL(net->eng, read_stats, 0, st);  // fires are counted by the neuron update itself
+        const double permille = 1000.0 * (double)(st[0] - net->auto_fires) / ((double)n * (double)m);
+        net->auto_fires = st[0];
+        if (net->eng.dense && permille < NC_AUTO_TO_EVENT_PERMILLE) NC_CALL(net->eng, set_form, false);
+        else if (!net->eng.dense && permille > NC_AUTO_TO_DENSE_PERMILLE) NC_CALL(net->eng, set_form, true);
+        n_steps -= m;
+    }
+    return NC_OK;
+}
+
 int nc_run(nc_net* net, int32_t n_steps)
 {
     NC_NEED_COUNTERS(net);
     if (n_steps < 0) return fail(NC_ERR_INVALID, "negative step count");
     if (net->step + n_steps >= (1ll << 30)) return fail(NC_ERR_INVALID, "step counter limit reached");
-    NC_CALL(net->eng, step, (int64_t)n_steps);
+    if (int rc = advance(net, n_steps)) return rc;
     net->step += n_steps;
     for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;  // currentTime = targetTime
+    return NC_OK;
+}
+
+int nc_get_step_form(nc_net* net, int32_t* form)
+{
+    if (!net || !form) return fail(NC_ERR_INVALID, "null argument");
+    *form = net->eng.dense ? NC_STEP_DENSE : NC_STEP_EVENT;
+    return NC_OK;
+}
+
+int nc_set_step_form(nc_net* net, int32_t form)
+{
+    NC_NEED(net);
+    if (form != NC_STEP_DENSE && form != NC_STEP_EVENT && form != NC_STEP_AUTO)
+        return fail(NC_ERR_INVALID, "unknown step form");
+    if (form == NC_STEP_AUTO) {
+        if (!net->eng.both) return fail(NC_ERR_UNSUPPORTED, "the network was not created with NC_STEP_AUTO");
+        unsigned long long st[4];
+        NC_CALL(net->eng, read_stats, 0, st);
+        net->auto_fires = st[0];
+        net->auto_form = true;
+        return NC_OK;
+    }
+    if (!net->eng.both && (form == NC_STEP_DENSE) != net->eng.dense)
+        return fail(NC_ERR_UNSUPPORTED, "the network holds the tables of its own form only (create it with NC_STEP_AUTO)");
+    NC_CALL(net->eng, set_form, form == NC_STEP_DENSE);
+    net->auto_form = false;
     return NC_OK;
 }
 
@@ -755,7 +806,26 @@ int nc_time_steps(nc_net* net, int32_t n_steps, float* ms, float* kernel_ms)
 {
     NC_NEED_COUNTERS(net);
     if (n_steps < 0 || !ms) return fail(NC_ERR_INVALID, "bad argument");
-    NC_CALL(net->eng, step_timed, (int64_t)n_steps, ms);
+    if (net->auto_form) {
+        // the window reads and any switch are part of the timed steps
+        cudaEvent_t a, b;
+        if (cudaEventCreate(&a) != cudaSuccess) return fail(NC_ERR_CUDA, "cudaEventCreate");
+        if (cudaEventCreate(&b) != cudaSuccess) {
+            cudaEventDestroy(a);
+            return fail(NC_ERR_CUDA, "cudaEventCreate");
+        }
+        cudaEventRecord(a, net->eng.stream);
+        int rc = advance(net, n_steps);
+        cudaEventRecord(b, net->eng.stream);
+        cudaError_t e = cudaEventSynchronize(b);
+        if (rc == NC_OK && e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (rc != NC_OK) return rc;
+        if (e != cudaSuccess) return fail(NC_ERR_CUDA, nc::cuda_msg("step timing", e));
+    } else {
+        NC_CALL(net->eng, step_timed, (int64_t)n_steps, ms);
+    }
     net->step += n_steps;
     for (int32_t k = 0; k < n_steps; ++k) net->time = net->time + net->host.dt;
     if (kernel_ms) {

@@ -52,6 +52,9 @@ int nc_batch_create(int32_t n_nets, const nc_net_spec* specs, nc_batch** out)
 {
     if (!out || n_nets <= 0 || !specs) return bfail(NC_ERR_INVALID, "bad arguments");
     *out = nullptr;
+    for (int32_t q = 0; q < n_nets; ++q)
+        if (specs[q].params.step_mode == NC_STEP_AUTO)
+            return bfail(NC_ERR_UNSUPPORTED, "NC_STEP_AUTO is for single networks; a batch runs in one form");
     int devices = 0;
     if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
         return bfail(NC_ERR_NODEVICE, "no CUDA device: the GB300 step has no CPU fallback");

@@ -242,6 +242,11 @@ int launch_step_dense(const NcPools& P, const LaunchShape& L, void* stream);
 // `ticks` whole dense steps of every net in one cooperative launch (no periodic input
 // firers); bar: two zero-initialised words of device memory for its grid barrier.
 int launch_fused_dense(const NcPools& P, int32_t ticks, unsigned* bar, void* stream);
+// Conversion of net `net`'s per-synapse arrival state between the forms (nc_form.cu),
+// after the current form's plasticity flush.  ring_words: the words of the whole ring
+// pool (cleared first).
+int launch_form_to_event(const NcPools& P, int net, int64_t n_syn, int64_t ring_words, void* stream);
+int launch_form_to_dense(const NcPools& P, int net, int64_t n_syn, void* stream);
 int launch_flush_dense(const NcPools& P, const LaunchShape& L, void* stream);
 int launch_background_prologue(const NcPools& P, int net, int n_neurons, void* stream);
 int launch_force_bits(const NcPools& P, int net, const int32_t* d_ids, int count, void* stream);

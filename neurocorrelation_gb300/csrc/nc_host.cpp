@@ -109,11 +109,11 @@ static void storage_order(NetHost& h, const float* xyz, int32_t order_kind)
 int64_t NetHost::device_bytes() const
 {
     const int64_t per_neuron = 4 + 4 + 4 + 4 + 8 + 8 + 4;             // pot lf firings act_start in_ptr out_ptr ring_off
-    const bool dense = p.step_mode == NC_STEP_DENSE;
-    // w t_arr term | csc_pre csc_post csc_dl la_c (dense) or out_post out_csc delay ringpos last_arr (event)
-    const int64_t per_syn = 4 + 4 + 8 + (dense ? 4 + 4 + 2 + 4 : 4 + 4 + 2 + 4 + 4);
+    const bool dense = p.step_mode != NC_STEP_EVENT, event = p.step_mode != NC_STEP_DENSE;
+    // w t_arr term | csc_pre csc_post csc_dl la_c (dense) and/or out_post out_csc delay ringpos last_arr (event)
+    const int64_t per_syn = 4 + 4 + 8 + (dense ? 4 + 4 + 2 + 4 : 0) + (event ? 4 + 4 + 2 + 4 + 4 : 0);
     const int64_t words = ((int64_t)n + 31) / 32;
-    const int64_t ring_bytes = dense ? 0 : 4 * (int64_t)ring_slots * ring_words;
+    const int64_t ring_bytes = event ? 4 * (int64_t)ring_slots * ring_words : 0;
     return per_neuron * (n + 1) + per_syn * s + ring_bytes + 4 * 4 * words +
            8 * 2 * (int64_t)n + 4 * (int64_t)tables.size() + (int64_t)sizeof(NcGroupDev) * (int64_t)groups.size();
 }
@@ -202,7 +202,7 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
         err = "unknown storage order";
         return NC_ERR_INVALID;
     }
-    if (p.step_mode != NC_STEP_DENSE && p.step_mode != NC_STEP_EVENT) {
+    if (p.step_mode != NC_STEP_DENSE && p.step_mode != NC_STEP_EVENT && p.step_mode != NC_STEP_AUTO) {
         err = "unknown step mode";
         return NC_ERR_INVALID;
     }

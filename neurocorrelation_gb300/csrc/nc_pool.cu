@@ -94,7 +94,9 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
     NC_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     int sms = 0;
     NC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    dense = nets.empty() || nets[0]->p.step_mode == NC_STEP_DENSE;
+    dense = nets.empty() || nets[0]->p.step_mode != NC_STEP_EVENT;
+    both = !nets.empty() && nets[0]->p.step_mode == NC_STEP_AUTO;
+    const bool event_tables = !dense || both;
     // the dense neuron pass is one wave: 128-thread blocks spread it more evenly over the
     // SMs (measured 2% faster on the 100k x 100 network than 256)
     L.neuron_block = dense ? NC_DNEURON_BLOCK : 256;
@@ -160,7 +162,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         ptrs += h.n + 1;
         words += sl.n_words;
         syn += (h.s + 31) / 32 * 32;  // keeps every net's inhibitory bits word-aligned
-        if (!dense) ring += (int64_t)h.ring_slots * h.ring_words;
+        if (event_tables) ring += (int64_t)h.ring_slots * h.ring_words;
         tables += (int64_t)h.tables.size();
         tiles += sl.n_words;
         spans += ((h.s + 31) / 32 + NC_SPAN_CHUNKS - 1) / NC_SPAN_CHUNKS;
@@ -193,7 +195,8 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         NC_ALLOC(P.pst, float, neurons);
         NC_ALLOC(P.win, uint32_t, syn / 32 + 1);
         NC_ALLOC(P.spans, NcTile, spans);
-    } else {
+    }
+    if (event_tables) {
         NC_ALLOC(P.out_ptr, int64_t, ptrs);
         NC_ALLOC(P.ring_off, int32_t, ptrs);
         NC_ALLOC(P.out_post, int32_t, syn);
@@ -202,13 +205,14 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         NC_ALLOC(P.out_ringpos, uint32_t, syn);
         NC_ALLOC(P.last_arr, int32_t, syn);
         NC_ALLOC(P.ring, uint32_t, ring);
+        ring_words_total_ = ring;
     }
     P.total_words = std::max<int64_t>(words, 1);
     NC_ALLOC(P.fired, uint32_t, 2 * P.total_words);
     NC_ALLOC(P.forced, uint32_t, 2 * P.total_words);
     NC_ALLOC(P.ufire, uint32_t, 2 * P.total_words);
-    P.fired_cap = dense ? 0 : std::max<int64_t>(neurons, 1);
-    if (!dense) NC_ALLOC(P.fired_list, int2, 2 * P.fired_cap);
+    P.fired_cap = event_tables ? std::max<int64_t>(neurons, 1) : 0;
+    if (event_tables) NC_ALLOC(P.fired_list, int2, 2 * P.fired_cap);
     NC_ALLOC(P.fired_count, int32_t, 2);
     NC_ALLOC(P.tables, float, tables);
     NC_ALLOC(P.groups, NcGroupDev, nets.size() * ngroups_each);
@@ -256,7 +260,8 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
             NC_CK(upload(P.la_c, never, sl.syn_base, stream));
             const int32_t chunks = (int32_t)((h.s + 31) / 32);
             for (int32_t c = 0; c < chunks; c += NC_SPAN_CHUNKS) span_host.push_back(NcTile{(int32_t)q, c});
-        } else {
+        }
+        if (event_tables) {
             NC_CK(upload(P.out_ptr, outp, sl.ptr_base, stream));
             NC_CK(upload(P.ring_off, h.ring_off, sl.ptr_base, stream));
             NC_CK(upload(P.last_arr, never, sl.syn_base, stream));
@@ -462,6 +467,27 @@ int Engine::flush_plasticity(std::string& err)
         return NC_ERR_CUDA;
     }
     return NC_OK;
+}
+
+int Engine::set_form(bool to_dense, std::string& err)
+{
+    if (to_dense == dense) return NC_OK;
+    if (!both || slots.size() != 1) {
+        err = "this network holds the tables of one form only (create it with NC_STEP_AUTO)";
+        return NC_ERR_UNSUPPORTED;
+    }
+    int rc = flush_plasticity(err);
+    if (rc != NC_OK) return rc;
+    rc = to_dense ? launch_form_to_dense(P, 0, slots[0].s, stream)
+                  : launch_form_to_event(P, 0, slots[0].s, ring_words_total_, stream);
+    if (rc) {
+        err = cuda_msg("form switch", cudaGetLastError());
+        return NC_ERR_CUDA;
+    }
+    release_graph();
+    dense = to_dense;
+    if (dense) prepare_dense_launch();
+    return sync(err);
 }
 
 int Engine::sync(std::string& err)

@@ -61,7 +61,12 @@ public:
     cudaStream_t stream = nullptr;
     int device = 0;
     int graph_ticks = 32;
-    bool dense = true;  // NC_STEP_DENSE: one launch per step (nc_dense.cu)
+    bool dense = true;  // the form the next steps run in: NC_STEP_DENSE (nc_dense.cu) or event
+    bool both = false;  // NC_STEP_AUTO: the tables of both forms are on the device
+    // Switches a single-net engine built with both forms' tables to the other form
+    // between steps (flushes the current form's deferred plasticity, converts the
+    // per-synapse arrival state, drops the captured graph).
+    int set_form(bool to_dense, std::string& err);
     // Launches one tick of the engine's form on `s` (no graph), the input firers' schedule
     // included.
     int launch_tick(cudaStream_t s);
@@ -84,6 +89,7 @@ private:
     int ids_cap_ = 0;
     unsigned long long* d_stats_ = nullptr;
     unsigned* d_bar_ = nullptr;  // grid barrier of the fused launch (arrivals, generation)
+    int64_t ring_words_total_ = 0;
 };
 
 std::string cuda_msg(const char* what, cudaError_t e);
