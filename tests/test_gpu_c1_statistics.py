@@ -13,9 +13,10 @@ diverge as chaotic trajectories do; what must agree is the statistics:
 
 * the population firing rate of every 1,000-step window within 1% of the reference's;
 * the final weight distribution: the Kolmogorov-Smirnov distance between the GPU's and
-  the reference's final weights (both quantised to 16 bits) at most 0.02.  The bound
-  is about ten times the distance between the reference's own runs of different seeds
-  on this workload (printed), so it catches a changed plasticity balance, not noise.
+  the reference's final weights (both quantised to 16 bits) no larger than the smallest
+  distance between two of the reference's own runs with different seeds (0.0135 on this
+  fixture; the GPU measures 0.001-0.003 against the same seed): a GPU run must be at
+  least as close to the reference as the reference is to itself under another seed.
 
 The fixture also holds the reference with its unmodified timing (lengths as built,
 background fires at random times inside the step) and with only the background times
@@ -29,7 +30,6 @@ from scenario import load
 
 pytestmark = pytest.mark.gpu
 
-KS_BOUND = 0.02
 RATE_TOL = 0.01
 
 
@@ -59,9 +59,9 @@ def c1_gpu(G, seed, mode):
 def test_gpu_c1_statistics_match_reference_run(nc, mode):
     fx = load("c1_reference_stats")
     seeds = [int(s) for s in fx["seeds"]]
-    spread = max(ks(fx[f"native_{a}_weights_u16"], fx[f"native_{b}_weights_u16"])
-                 for i, a in enumerate(seeds) for b in seeds[i + 1:])
-    print(f"\nreference seed-to-seed KS distance of the final weights: {spread:.4f}")
+    bound = min(ks(fx[f"native_{a}_weights_u16"], fx[f"native_{b}_weights_u16"])
+                for i, a in enumerate(seeds) for b in seeds[i + 1:])
+    print(f"\nsmallest seed-to-seed KS distance of the reference's final weights: {bound:.4f}")
     for s in seeds:
         rates, wq = c1_gpu(nc, s, mode)
         ref = fx[f"native_{s}_pop_rate_hz"]
@@ -70,7 +70,7 @@ def test_gpu_c1_statistics_match_reference_run(nc, mode):
         print(f"seed {s}: rate GPU {rates.mean():.2f} Hz, reference {ref.mean():.2f} Hz, "
               f"worst window {rel.max() * 100:.3f}%; KS {d:.4f}")
         assert rel.max() <= RATE_TOL, (s, rates, ref)
-        assert d <= KS_BOUND, (s, d)
+        assert d <= bound, (s, d, bound)
     for timing in ("continuous", "continuous_grid"):
         ref = fx[f"{timing}_{seeds[0]}_pop_rate_hz"]
         rates, wq = c1_gpu(nc, seeds[0], mode)

@@ -145,3 +145,36 @@ def test_background_draw_rate(oracle_mod):
         hits += int(h.sum())
         assert tgt.min() >= 0 and tgt.max() < 3000
     assert abs(hits / (200 * 3000) - 1 / 600) < 0.0005
+
+
+def _ks(a, b):
+    a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
+    v = np.union1d(a, b)
+    return float(np.max(np.abs(np.searchsorted(a, v, "right") / a.size - np.searchsorted(b, v, "right") / b.size)))
+
+
+def test_oracle_c1_statistics_match_reference_run(oracle_mod):
+    """The oracle (bit-identical to the GPU) against the reference's own NeuCor::run with
+    every event on the step grid, 1,000-neuron / 50k-synapse workload, 10,000 steps, one
+    seed: every 1,000-step window's population rate within 1%, final-weight KS distance no
+    larger than the reference's own between two seeds (tests/test_gpu_c1_statistics.py
+    runs all seeds on the GPU)."""
+    O = oracle_mod
+    fx = load("c1_reference_stats")
+    seed = int(fx["seeds"][0])
+    xyz, pre, post, w = O.build_knn(1000, 50, 8.0, 1)
+    groups = [dict(first=0, count=10, rate_hz=20.0, correlated=1, jitter=2),
+              dict(first=10, count=10, rate_hz=20.0, correlated=0, jitter=0)]
+    o = O.OracleS(xyz, pre, post, w, params=O.default_params(seed=seed), groups=groups)
+    rates = []
+    for _ in range(10):
+        f0 = o.stats()["fires"]
+        o.run(1000)
+        rates.append((o.stats()["fires"] - f0) / 1000.0)
+    ref = fx[f"native_{seed}_pop_rate_hz"]
+    assert np.max(np.abs(np.asarray(rates) - ref) / ref) <= 0.01
+    wq = np.rint(np.clip(o.weights(), 0.0, 1.0) * 65535.0).astype(np.uint16)
+    s = [int(x) for x in fx["seeds"]]
+    bound = min(_ks(fx[f"native_{a}_weights_u16"], fx[f"native_{b}_weights_u16"])
+                for i, a in enumerate(s) for b in s[i + 1:])
+    assert _ks(wq, fx[f"native_{seed}_weights_u16"]) <= bound
