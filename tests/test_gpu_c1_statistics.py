@@ -8,8 +8,8 @@ oracle/ref_harness.cpp; tests/golden/make_golden.py, section c1_stats) with ever
 on the step grid: runAll, synapse lengths of whole-step delays (the benchmark spec's integer
 delays) and background fire times on the step boundary.  Its per-window population
 rates and final weights are the fixture.  The GPU and the reference compute the same
-bits until the first same-step order coincidence (a few hundred steps here), then
-diverge as chaotic trajectories do; what must agree is the statistics:
+bits until the first same-step order coincidence, then diverge as chaotic trajectories
+do; what must agree is the statistics:
 
 * the population firing rate of every 1,000-step window within 1% of the reference's;
 * the final weight distribution: the Kolmogorov-Smirnov distance between the GPU's and
@@ -20,9 +20,11 @@ diverge as chaotic trajectories do; what must agree is the statistics:
 
 The fixture also holds the reference with its unmodified timing (lengths as built,
 background fires at random times inside the step) and with only the background times
-off the grid.  Both depart from the fixed-step model by the same amount (printed; the
-design notes explain why): the reference's charge per run, deltaT*exp(0.3702*deltaT),
-depends on how often a neuron is run, which off-grid events change."""
+off the grid.  Both depart from the fixed-step model alike (printed): the departure comes
+with off-grid event times, not with the rounding of delays.  In the reference's code an
+arrival re-runs its target at once (transfer, src/NeuCor.cpp:663-666) and a run adds
+deltaT*depolFac*0.9943*exp(0.3702*deltaT) per active synapse (:695), which depends on how
+often the neuron is run."""
 import numpy as np
 import pytest
 
