@@ -78,10 +78,11 @@ typedef struct {
 #define NC_ORDER_ID 1
 
 /* Form of the step kernels.  Results never depend on it.
- *   NC_STEP_DENSE  (default) one launch per step; each warp walks its 32 targets'
- *                  in-synapse rows in order, making the launch decisions, the plasticity
- *                  and the arrival window there.  Its cost grows with the synapse count:
- *                  the faster form when a large share of neurons fires every step.
+ *   NC_STEP_DENSE  (default) two launches per step: a synapse pass that streams every
+ *                  in-synapse row in order, making the launch decisions, the plasticity
+ *                  and the arrival window there, and a neuron pass.  Its cost grows with
+ *                  the synapse count: the faster form when a large share of neurons fires
+ *                  every step.
  *   NC_STEP_EVENT  two launches per step; fired neurons are compacted into a list and
  *                  only their out-synapses and the arrived spikes are touched.  Its cost
  *                  grows with the synaptic events: the faster form for sparse activity.
