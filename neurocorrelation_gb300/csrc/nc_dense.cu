@@ -363,13 +363,17 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                             const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
                             const bool arrived = la == prev_c;
                             const int32_t after = (int32_t)((dl >> 14) & 1u);
-                            launch = srcf && (la == NC_NEVER || prev_c - la >= C.kc + after);
+                            // free: never launched (NC_NEVER is INT32_MIN, far below) or
+                            // prev - la >= KC + after
+                            launch = srcf && la + C.kc + after <= prev_c;
                             nl += launch;
                             nd += srcf && !launch;
                             const bool ih = (ihw[u] >> lane) & 1u;
+                            const float lo = ih ? -1.0f : 0.0f, hi = ih ? 0.0f : 1.0f;
                             const float w0 = B.w[q];
                             float w1 = w0;
-                            if (tf) w1 = plasticity(w0, ih, trace_at(C.tab_pre, C.tab_pre_len, prev_c, B.ta[q]), 0.0f, C.R);
+                            if (tf) w1 = plasticity_b(w0, lo, hi, trace_at_u(C.tab_pre, C.tab_pre_len, prev_c, B.ta[q]),
+                                                      0.0f, C.R);
                             if (launch) {
                                 // target below the source in caller order and fired at prev:
                                 // its update ran first, post-spike plasticity included
@@ -382,13 +386,14 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                             float w2 = w1;
                             if (arrived) {
                                 // the target's post trace at prev (0 when it fired at prev)
-                                w2 = plasticity(w1, ih, 0.0f, fabsf(pstv[u]), C.R);
+                                w2 = plasticity_b(w1, lo, hi, 0.0f, fabsf(pstv[u]), C.R);
                                 ta_u[q] = prev_c;
                             }
                             if (tf || arrived) w_u[q] = w2;
                         }
-                        // arrived t-KC .. t-1: in the fold of step t
-                        const bool win = lac != NC_NEVER && C.t - lac >= 1 && C.t - lac <= C.kc;
+                        // arrived t-KC .. t-1: in the fold of step t (NC_NEVER and later
+                        // arrivals wrap past KC)
+                        const bool win = (uint32_t)prev_c - (uint32_t)lac < (uint32_t)C.kc;
                         const uint32_t wm = __ballot_sync(kFull, win);
                         if (lane == 0 && (h + u) * 32 < u_rem) win_u[h + u] = wm;
                         const uint32_t lm = __ballot_sync(kFull, launch);

@@ -51,6 +51,26 @@ static __device__ __forceinline__ float plasticity(float w, bool inh, float trac
     return v;
 }
 
+// The same update with the clamp bounds of the synapse's sign given: hi = 1, lo = 0 for an
+// excitatory synapse, hi = 0, lo = -1 for an inhibitory one (the same compares and
+// selects as above, with the bounds chosen once per synapse).
+static __device__ __forceinline__ float plasticity_b(float w, float lo, float hi, float traceS, float traceT,
+                                                     const Rates& R)
+{
+    const float weightChange = R.pre * traceS - R.post * traceT;
+    const float v = w + weightChange * R.lr;
+    const float m = (v <= hi) ? v : hi;
+    return (m >= lo) ? m : lo;
+}
+
+// trace_at with one unsigned compare: a step counter `then` of NC_NEVER (INT32_MIN) puts
+// now - then at 2^31 or above, past any table.
+static __device__ __forceinline__ float trace_at_u(const float* tab, int len, int32_t now, int32_t then)
+{
+    const uint32_t k = (uint32_t)now - (uint32_t)then;
+    return k < (uint32_t)len ? __ldg(tab + k) : 0.0f;
+}
+
 static __device__ __forceinline__ float plasticity(float w, bool inh, float traceS, float traceT, const NcNetDesc& D)
 {
     return plasticity(w, inh, traceS, traceT, rates_of(D));
