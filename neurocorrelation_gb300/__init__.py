@@ -23,7 +23,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_lib", "libneucor_gb300.so")
 
 NC_OK = 0
-NC_STEP_DENSE = 0  # step_mode: one launch per step, in-rows walked in order
+NC_STEP_DENSE = 0  # step_mode: a synapse pass walking the in-rows in order, then a neuron pass
 NC_STEP_EVENT = 1  # step_mode: fired-list compaction and spike launch (sparse activity)
 NC_STEP_AUTO = 2   # step_mode: both forms' tables; nc_run switches by the fire share
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "no CUDA device",

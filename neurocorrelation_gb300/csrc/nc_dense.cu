@@ -8,8 +8,7 @@
 //
 //   k_dense_synapses (warp per span of 8 x 32 in-synapses, CSC order; the span's
 //   streams arrive by bulk copies into shared memory, the next ones in flight while a
-//   warp works; k_dense_synapses_direct is the same pass on register loads), for the
-//   step prev = t-1 of the span's net:
+//   warp works), for the step prev = t-1 of the span's net:
 //     Synapse::fire of every in-synapse whose source fired at prev (src/NeuCor.cpp:
 //     727-738): dropped while busy, otherwise it captures fl(fl(0.2f*52)*w) and its
 //     arrival step; then the plasticity of prev (src/NeuCor.cpp:740-761): post-spike
@@ -19,7 +18,10 @@
 //     ballot of "arrived in t-KC .. t-1" is one word of the window bitmap.
 //   k_dense_neurons (lane per neuron): charge_insynapses in ascending source order
 //     from the window bitmap, charge_passive, threshold, AP, background draws (as the
-//     event form's k_neuron_step); a neuron inside its AP skips its fold.
+//     event form's k_neuron_step); a neuron inside its AP skips its fold.  It also
+//     writes each neuron's post state for the next synapse pass.
+//   k_dense_fused: both passes of several steps in one cooperative launch, with grid
+//     barriers between them (batched engines).
 //
 // Launches of the fires of prev happen at the start of step t instead of the end of
 // step prev; nothing between those points reads what they write (a spike launched at

@@ -1,7 +1,7 @@
 """GPU step (libneucor_gb300.so through the C ABI) against the reference's own outputs
 (golden fixtures) and against the stepped CPU restatement (oracle), bit for bit:
 spike rasters, potentials, weights, activities, last-fire times and counters.  Every
-case runs in both forms of the step kernels (dense: one launch per step walking the
+case runs in both forms of the step kernels (dense: a synapse pass walking the
 in-rows; event: fired-list compaction and spike launch)."""
 import numpy as np
 import pytest
