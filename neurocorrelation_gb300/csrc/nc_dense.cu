@@ -532,6 +532,10 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
 // The neuron pass of every tile (see k_dense_neurons), each block striding over groups
 // of tiles; the last block to finish advances the nets' step counters.  All threads of
 // the block call it.
+#ifndef NC_NEURON_EARLY
+#define NC_NEURON_EARLY 1
+#endif
+
 __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
 {
     int* s_net = sh.s_net;
@@ -549,6 +553,11 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
         // which of the block's neurons fold, packed in tile order
         const int tix = tb * wpb + wib;
         bool need = false;
+        // NC_NEURON_EARLY: the input requests and the background draw of each lane, which
+        // do not depend on its potential, are made before the block's folds, so the warps
+        // that do not fold make them while the others fold
+        bool early_req = false;
+        uint32_t early_bg = ~0u;  // slot of the background target for t+1, or ~0u
         if (tix < n_tiles) {
             const NcTile tile = P.tiles[tix];
             const NcNetDesc& D = P.nets[tile.net];
@@ -558,6 +567,20 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
                 const int32_t lf = P.lf[D.neuron_base + j];
                 need = !(lf != NC_NEVER && t - lf < D.kc) &&
                        P.in_ptr[D.ptr_base + j + 1] > P.in_ptr[D.ptr_base + j];
+                if (NC_NEURON_EARLY) {
+                    const int32_t pj = D.neuron_base + j;
+                    const int32_t cid = D.permuted ? P.orig_id[pj] : j;
+                    if (D.n_groups) early_req = input_request(P, D, cid, t);
+                    if (D.bg_period > 0) {
+                        uint32_t o[4];
+                        philox((uint32_t)cid, (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
+                        if (o[0] % (uint32_t)D.bg_period == 0u) {
+                            uint32_t tgt = o[1] % (uint32_t)D.n;
+                            if (D.permuted) tgt = (uint32_t)P.slot_of[D.neuron_base + tgt];
+                            early_bg = tgt;
+                        }
+                    }
+                }
             }
         }
         const uint32_t need_m = __ballot_sync(kFull, need);
@@ -601,7 +624,8 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
             const uint32_t fw = P.forced[(int64_t)(t & 1) * P.total_words + word];
             const uint32_t uw = P.ufire[(int64_t)(t & 1) * P.total_words + word];
             bool forced = (fw >> lane) & 1u;
-            if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
+            if (NC_NEURON_EARLY) forced = forced || early_req;
+            else if (!forced && D.n_groups) forced = input_request(P, D, D.permuted ? P.orig_id[pj] : j, t);
             // charge_passive (src/NeuCor.cpp:677-680)
             pot = (pot - -70.0f) * D.leak + -70.0f;
             // charge_thresholdCheck (src/NeuCor.cpp:682-686); vesicles stay positive
@@ -630,7 +654,10 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
         }
         acc[0] += (unsigned long long)__popc(fmask);
         // background fires for step t+1 (src/NeuCor.cpp:604-607), drawn per caller id
-        if (live && D.bg_period > 0) {
+        if (NC_NEURON_EARLY && early_bg != ~0u)
+            atomicOr(P.forced + (int64_t)((t + 1) & 1) * P.total_words + D.word_base + (early_bg >> 5),
+                     1u << (early_bg & 31));
+        if (!NC_NEURON_EARLY && live && D.bg_period > 0) {
             uint32_t o[4];
             philox((uint32_t)(D.permuted ? P.orig_id[pj] : j), (uint32_t)t, NC_STREAM_BACKGROUND, 0u, D, o);
             if (o[0] % (uint32_t)D.bg_period == 0u) {
