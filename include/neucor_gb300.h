@@ -205,8 +205,9 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* neuron_ids);
 /* ------------------------------------------------------------------ run */
 /* Advances n_steps steps (NeuCor::run called n_steps times, src/NeuCor.cpp:583-617).
  * Asynchronous on the handle's stream; read-backs synchronise.  A network in
- * NC_STEP_AUTO runs in windows of NC_AUTO_WINDOW steps and reads its fire count after
- * each (a synchronisation): it moves to the event form when fewer than
+ * NC_STEP_AUTO runs in windows of NC_AUTO_WINDOW steps (a window may span several run
+ * calls) and reads its fire count at the end of each (a synchronisation): it moves to
+ * the event form when fewer than
  * NC_AUTO_TO_EVENT_PERMILLE per mille of its neurons fired per step in the window, and
  * back to the dense form above NC_AUTO_TO_DENSE_PERMILLE (the measured crossover of the
  * two forms on a 100k-neuron, 100-fan-out network lies between). */

@@ -437,8 +437,10 @@ int nc_schedule_fire(nc_net* net, int32_t count, const int32_t* ids)
     return NC_OK;
 }
 
-// Steps the engine; a network in NC_STEP_AUTO runs window by window and, after each,
-// moves to the form its fire share calls for (NC_AUTO_* in neucor_gb300.h).
+// Steps the engine; a network in NC_STEP_AUTO runs window by window (a window may span
+// run calls, so single-step calls synchronise once per window, not per call) and, at
+// the end of each, moves to the form its fire share calls for (NC_AUTO_* in
+// neucor_gb300.h).
 static int advance(nc_net* net, int64_t n_steps)
 {
     if (!net->auto_form) {
@@ -447,15 +449,19 @@ static int advance(nc_net* net, int64_t n_steps)
     }
     const int32_t n = std::max(net->host.n, 1);
     while (n_steps > 0) {
-        const int64_t m = std::min<int64_t>(n_steps, NC_AUTO_WINDOW);
+        const int64_t m = std::min<int64_t>(n_steps, NC_AUTO_WINDOW - net->auto_steps);
         NC_CALL(net->eng, step, m);
+        net->auto_steps += m;
+        n_steps -= m;
+        if (net->auto_steps < NC_AUTO_WINDOW) continue;
         unsigned long long st[4];
         NC_CALL(net->eng, read_stats, 0, st);  // fires are counted by the neuron update itself
-        const double permille = 1000.0 * (double)(st[0] - net->auto_fires) / ((double)n * (double)m);
+        const double permille =
+            1000.0 * (double)(st[0] - net->auto_fires) / ((double)n * (double)net->auto_steps);
         net->auto_fires = st[0];
+        net->auto_steps = 0;
         if (net->eng.dense && permille < NC_AUTO_TO_EVENT_PERMILLE) NC_CALL(net->eng, set_form, false);
         else if (!net->eng.dense && permille > NC_AUTO_TO_DENSE_PERMILLE) NC_CALL(net->eng, set_form, true);
-        n_steps -= m;
     }
     return NC_OK;
 }
@@ -488,6 +494,7 @@ int nc_set_step_form(nc_net* net, int32_t form)
         unsigned long long st[4];
         NC_CALL(net->eng, read_stats, 0, st);
         net->auto_fires = st[0];
+        net->auto_steps = 0;
         net->auto_form = true;
         return NC_OK;
     }

@@ -13,10 +13,12 @@ struct nc_net {
     // them, so from then on step and time are read back from the device's step
     // counter (NcNetDesc t, tsum) before any call that uses them.
     bool counters_on_device = false;
-    // NC_STEP_AUTO: nc_run picks the form from the last window's fires (auto_form), and
-    // auto_fires is the fire count at the end of the last window
+    // NC_STEP_AUTO: nc_run picks the form from the last window's fires (auto_form);
+    // auto_fires is the fire count at the start of the current window and auto_steps the
+    // steps run in it so far (windows span run calls)
     bool auto_form = false;
     uint64_t auto_fires = 0;
+    int64_t auto_steps = 0;
     uint32_t* d_raster = nullptr;
     uint32_t* d_raster_ids = nullptr;  // the same rows in caller-id order (read-back staging)
     int32_t raster_cap = 0;

@@ -70,6 +70,22 @@ def test_auto_policy_picks_the_form_by_activity(nc, oracle_mod):
         assert (st["fires"], st["launched"], st["dropped"]) == (so["fires"], so["launched"], so["dropped"])
 
 
+def test_auto_window_spans_single_step_calls(nc, oracle_mod):
+    """A caller stepping one step per run call (as the renderer does) still gets the
+    automatic choice: the windows span the calls."""
+    G, O = nc, oracle_mod
+    xyz, pre, post, w = G.build_knn(2000, 30, 8.0, seed=4)
+    ws = (w * np.float32(0.02)).astype(np.float32)
+    net = G.NeuCor.from_arrays(xyz, pre, post, ws, params=G.default_params(seed=6, step_mode=AUTO))
+    for _ in range(600):
+        net.run(1)
+    assert net.step_form == EVENT
+    o = O.OracleS(xyz, pre, post, ws, params=O.default_params(seed=6))
+    o.run(600)
+    np.testing.assert_array_equal(bits(net.potentials()), bits(o.potentials()))
+    np.testing.assert_array_equal(bits(net.weights()), bits(o.weights()))
+
+
 def test_single_form_networks_refuse_a_switch(nc):
     G = nc
     xyz, pre, post, w = knn_net(64, 4, 3)
