@@ -152,8 +152,23 @@ struct NetConst {                 // a span's net constants (see the staged pass
     Rates R;
 };
 
+// Lane 0's memo of the last span and net it staged: the second half of a span, and
+// every span of a net after its first, are issued without reloading the span table
+// and the net's descriptor (two dependent loads ahead of the copies).
+// (Kept in the warp's shared memory: only lane 0 uses it.)
+struct StageMemo {
+    int64_t base;    // syn_base
+    int64_t chunks;  // 32-synapse chunks of the net
+    NcTile span;
+    int sp;
+    int net;
+    int ok;          // the net runs its synapse pass in this launch
+    int pad;
+};
+
 struct __align__(16) WarpStage {
     StageBuf buf[kStages];
+    StageMemo memo;
     NetConst nc;
     unsigned long long bar[kStages];  // mbarriers: the copies of buf[k] have landed
     int32_t qs[kQueue];               // launched synapse, relative to its span's first
@@ -174,20 +189,33 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
                  :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
+#ifndef NC_STAGE_MEMO
+#define NC_STAGE_MEMO 1
+#endif
+
 // Lane 0: copies unit `half` of span `sp` into b (all six streams), completing on *bar.
 // Returns 0 when nothing is copied: the span's net is skipped this launch, or the unit
 // lies past the net's last synapse.
-__device__ int stage_unit(const NcPools& P, int sp, int half, bool flush, StageBuf* b, unsigned long long* bar)
+__device__ int stage_unit(const NcPools& P, int sp, int half, bool flush, StageBuf* b, unsigned long long* bar,
+                          StageMemo& m)
 {
-    const NcTile span = P.spans[sp];
-    const NcNetDesc& D = P.nets[span.net];
-    const int32_t t = D.t, prev = t - 1;
-    if (!D.active || prev < 1 || D.stdp_done >= prev || (!flush && t > D.t_end)) return 0;
-    const int64_t chunks = (D.n_syn + 31) / 32;
-    const int64_t c0 = span.first + (int64_t)half * kUnitChunks;
-    const int64_t nch = min((int64_t)kUnitChunks, chunks - c0);
+    if (!NC_STAGE_MEMO || sp != m.sp) {
+        m.span = P.spans[sp];
+        m.sp = sp;
+    }
+    if (!NC_STAGE_MEMO || m.span.net != m.net) {
+        const NcNetDesc& D = P.nets[m.span.net];
+        const int32_t t = D.t, prev = t - 1;
+        m.ok = D.active && prev >= 1 && D.stdp_done < prev && (flush || t <= D.t_end);
+        m.base = D.syn_base;
+        m.chunks = (D.n_syn + 31) / 32;
+        m.net = m.span.net;
+    }
+    if (!m.ok) return 0;
+    const int64_t c0 = m.span.first + (int64_t)half * kUnitChunks;
+    const int64_t nch = min((int64_t)kUnitChunks, m.chunks - c0);
     if (nch <= 0) return 0;
-    const int64_t s = D.syn_base + c0 * 32;
+    const int64_t s = m.base + c0 * 32;
     const uint32_t b4 = (uint32_t)(nch * 128), b2 = (uint32_t)(nch * 64);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)), "r"(5 * b4 + b2)
                  : "memory");
@@ -250,10 +278,16 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
     // unit k of this warp: half k % kUnitsPerSpan of span gw + (k / kUnitsPerSpan) * nw,
     // staged in slot k % kStages
     int iss = 0;  // lane 0: bit j set = slot j holds an issued unit not yet consumed
+    StageMemo& memo = ws.memo;
+    if (lane == 0) {
+        memo.sp = -1;
+        memo.net = -1;
+    }
     if (lane == 0)
         for (int k = 0; k < kStages - 1; ++k) {
             const int sp = gw + (k / kUnitsPerSpan) * nw;
-            if (sp < n_spans && stage_unit(P, sp, k % kUnitsPerSpan, kFlush, &ws.buf[k], &ws.bar[k])) iss |= 1 << k;
+            if (sp < n_spans && stage_unit(P, sp, k % kUnitsPerSpan, kFlush, &ws.buf[k], &ws.bar[k], memo))
+                iss |= 1 << k;
         }
 
     int acc_net = -1, cur_net = -1;
@@ -311,7 +345,8 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                 const int spn = gw + (kn / kUnitsPerSpan) * nw;
                 if (lane == 0) {
                     iss &= ~(1 << sn);
-                    if (spn < n_spans && stage_unit(P, spn, kn % kUnitsPerSpan, kFlush, &ws.buf[sn], &ws.bar[sn]))
+                    if (spn < n_spans &&
+                        stage_unit(P, spn, kn % kUnitsPerSpan, kFlush, &ws.buf[sn], &ws.bar[sn], memo))
                         iss |= 1 << sn;
                 }
             }
