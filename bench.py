@@ -558,7 +558,11 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel_ms": kernels,
-                     "events_per_step_in_kernel_pass": ev_per_step_k},
+                     "events_per_step_in_kernel_pass": ev_per_step_k,
+                     # the DRAM bytes the kernel actually moves (ncu, per launch) over its
+                     # CUDA-event time: how well it uses HBM, beside the algorithmic fraction
+                     "traffic_gbs": traffic / dur / 1e9 if traffic else None,
+                     "traffic_frac": traffic / dur / 1e9 / peak if traffic else None},
         "e2e": {"value": tot_e2e / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
     }
