@@ -50,6 +50,37 @@ def test_forced_switches_match_oracle(nc, oracle_mod, label, make, pkw, groups):
     np.testing.assert_array_equal(bits(net.potAct[1::2]), bits(o.activity()))
 
 
+def test_forced_switches_with_firers_and_detectors(nc, oracle_mod):
+    """Periodic input firers (their fires land in the next step's input bits, shared by
+    both forms) and detectors across form switches: raster and potentials every step
+    equal the oracle's."""
+    G, O = nc, oracle_mod
+    xyz, pre, post, w = knn_net(250, 10, 64, inhibitory=0.1)
+    pkw = dict(seed=81, run_speed=0.5)
+    net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(**pkw, step_mode=AUTO))
+    o = O.OracleS(xyz, pre, post, w, params=O.default_params(**pkw))
+    rates = np.array([40.0, 125.0, 70.0], np.float32)
+    fxyz = xyz[[3, 80, 170]]
+    frad = np.array([0.6, 0.9, 0.5], np.float32)
+    net.setInputRateArray(rates, inputPositions=fxyz, inputRadius=frad)
+    o.set_firers(rates, fxyz, frad)
+    net.setDetectors(2, xyz[[10, 200]], np.array([0.8, 1.1], np.float32))
+    plan = [(EVENT, 23), (DENSE, 5), (EVENT, 1), (DENSE, 40), (EVENT, 31)]
+    total = sum(m for _, m in plan)
+    net.record_raster(total)
+    rows = []
+    for form, m in plan:
+        net.set_step_form(form)
+        for _ in range(m):
+            net.run(1)
+            r, p = o.run(1, raster=True, pots=True)
+            rows.append(r[0])
+            np.testing.assert_array_equal(bits(net.potentials()), bits(p[0]))
+        assert len(net.getDetectorVoltages()) == 2
+    np.testing.assert_array_equal(net.raster(), np.asarray(rows))
+    np.testing.assert_array_equal(bits(net.weights()), bits(o.weights()))
+
+
 def test_auto_policy_picks_the_form_by_activity(nc, oracle_mod):
     """A saturated network stays dense; the same network with weak synapses (quiet)
     moves to the event form on its own; both stay equal to the oracle."""
