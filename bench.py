@@ -257,10 +257,11 @@ def c3_nets(G, n_nets, horizon, seed=3):
     return nets
 
 
-def c4_requests(G, n_req, horizon_scale, seed=4):
+def c4_requests(n_req, horizon_scale, seed=4):
     """Served workload: Poisson arrivals at 50 requests/s; sizes log-uniform over
     500-200k neurons, fan-out 20-150, horizons log-uniform over 1k-100k steps (times
-    horizon_scale), each with a random input pattern of 1-8 groups."""
+    horizon_scale), each with a random input pattern of 1-8 groups.  A request is the
+    parameters of its kNN network (the server builds it)."""
     rng = np.random.default_rng(seed)
     t, reqs = 0.0, []
     for q in range(n_req):
@@ -272,8 +273,7 @@ def c4_requests(G, n_req, horizon_scale, seed=4):
         groups = [dict(first=10 * g, count=10, rate_hz=float(rng.uniform(5.0, 50.0)), correlated=int(rng.integers(0, 2)),
                        jitter=int(rng.integers(0, 4))) for g in range(ng)]
         nseed = seed * 100003 + q
-        xyz, pre, post, w = G.build_knn(n, k, 8.0, seed=nseed)
-        reqs.append(dict(xyz=xyz, pre=pre, post=post, weight=w, seed=nseed, groups=groups, horizon=h, arrival=t))
+        reqs.append(dict(knn=(n, k, nseed), seed=nseed, groups=groups, horizon=h, arrival=t))
     return reqs
 
 
@@ -284,8 +284,12 @@ def one_at_a_time(G, nets, mode, arrivals=None):
     events, busy, run_s, clock, lat = 0, 0.0, 0.0, 0.0, []
     for q, d in enumerate(nets):
         t0 = time.perf_counter()
-        net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"],
-                                   params=G.default_params(seed=d["seed"], step_mode=mode))
+        if "knn" in d:  # the drop-in's own kNN construction (on the device in the dense form)
+            n, k, kseed = d["knn"]
+            net = G.NeuCor.knn(n, k, 8.0, seed=kseed, params=G.default_params(seed=d["seed"], step_mode=mode))
+        else:
+            net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"],
+                                       params=G.default_params(seed=d["seed"], step_mode=mode))
         net.set_input_groups(d["groups"])
         net.sync()
         t1 = time.perf_counter()
@@ -340,7 +344,7 @@ def measure_batched(G, n_nets, horizon, mode, one_at_a_time_sample=None):
 
 
 def measure_served(G, n_req, horizon_scale, budget, mode):
-    reqs = c4_requests(G, n_req, horizon_scale)
+    reqs = c4_requests(n_req, horizon_scale)
     srv = G.Server(budget, max_networks=256, steps_per_batch=64, build_threads=min(16, os.cpu_count() or 1),
                    step_mode=mode)
     t0 = time.perf_counter()
@@ -348,9 +352,9 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
         wait = t0 + r["arrival"] - time.perf_counter()
         if wait > 0:
             time.sleep(wait)
-        srv.submit(dict(xyz=r["xyz"], pre=r["pre"], post=r["post"], weight=r["weight"],
-                        params=G.default_params(seed=r["seed"], step_mode=mode), groups=r["groups"],
-                        horizon=r["horizon"]))
+        n, k, kseed = r["knn"]
+        srv.submit_knn(n, k, 8.0, kseed, r["horizon"], params=G.default_params(seed=r["seed"], step_mode=mode),
+                       groups=r["groups"])
     srv.drain()
     done = srv.poll()
     sst = srv.stats()
@@ -359,10 +363,15 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
     lat = np.array([d["done_s"] - d["submit_s"] for d in ok])
     span = max(d["done_s"] for d in ok) - min(d["submit_s"] for d in ok)
     events = sum(d["launched"] for d in ok)
+    t_one = time.perf_counter()
     ev1, busy1, _, lat1 = one_at_a_time(G, reqs, mode, arrivals=[r["arrival"] for r in reqs])
     span1 = max(a + l for a, l in zip([r["arrival"] for r in reqs], lat1)) - reqs[0]["arrival"]
+    t_end = time.perf_counter()
     return {"workload": f"{n_req} requests, Poisson arrivals at 50/s, 500-200k neurons, fan-out 20-150, "
-                        f"horizons log-uniform 1k-100k steps x {horizon_scale}, 1-8 input groups each",
+                        f"horizons log-uniform 1k-100k steps x {horizon_scale}, 1-8 input groups each; "
+                        "served: each sent as kNN parameters and built by the server's builder threads; "
+                        "one at a time: each built by the drop-in's device kNN builder, run and read back",
+            "wall_s": {"served": t_one - t0, "one_at_a_time": t_end - t_one},
             "requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
             "budget_gb": budget / 1e9, "events_per_s": events / span, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "peak_resident_networks": sst["peak_resident_networks"],

@@ -377,7 +377,9 @@ typedef struct {
     int64_t memory_budget_bytes; /* device memory for resident networks */
     int32_t max_networks;        /* networks resident at once */
     int32_t steps_per_batch;     /* steps between admission / completion decisions */
-    int32_t build_threads;       /* host threads preparing submitted networks */
+    int32_t build_threads;       /* host threads preparing submitted networks; they pause while the
+                                    prepared, not yet admitted requests hold more than 8 GiB of
+                                    host tables */
     int32_t keep_results;        /* 1: keep finished networks' weights and potentials for nc_server_fetch */
     int32_t step_mode;           /* NC_STEP_*: form of the step kernels for every request */
 } nc_server_config;
@@ -408,6 +410,13 @@ int nc_server_create(const nc_server_config* config, nc_server** out);
 /* Copies the spec's arrays; returns at once.  NC_ERR_BUDGET if the network could never
  * fit the budget. */
 int nc_server_submit(nc_server* server, const nc_net_spec* spec, int64_t* request_id);
+/* A request for the kNN network nc_build_knn(n, k, density, knn_seed) describes (the
+ * workloads' networks), built by one of the server's builder threads: the caller sends
+ * parameters only, and the network's arrays exist only while that thread prepares it.
+ * No counterpart in the reference. */
+int nc_server_submit_knn(nc_server* server, int32_t n, int32_t k, float density, uint64_t knn_seed,
+                         const nc_params* params, int32_t n_groups, const nc_group* groups, int32_t horizon,
+                         int64_t* request_id);
 /* Finished requests since the last poll (at most `capacity`). */
 int nc_server_poll(nc_server* server, nc_request_done* out, int32_t capacity, int32_t* count);
 /* Blocks until every submitted request has finished. */

@@ -137,6 +137,7 @@ def load_library() -> ctypes.CDLL:
         "nc_server_poll": ([P, P, I32, P], I32), "nc_server_drain": ([P], I32),
         "nc_server_fetch": ([P, I64, P, P], I32), "nc_server_get_stats": ([P, P], I32),
         "nc_server_destroy": ([P], I32), "nc_run_noalloc": ([P, I32, P], I32),
+        "nc_server_submit_knn": ([P, I32, I32, F, ctypes.c_uint64, P, I32, P, I32, P], I32),
         "nc_set_input_rates": ([P, I32, P], I32), "nc_add_input_offset": ([P, I32, F], I32),
         "nc_set_detectors": ([P, I32, P, P], I32), "nc_get_detector_voltages": ([P, P, I32, P], I32),
         "nc_get_detector_voltage": ([P, I32, P], I32),
@@ -782,6 +783,22 @@ class Server:
         rid = ctypes.c_int64()
         _check(self._lib.nc_server_submit(self._h, ctypes.byref(spec), ctypes.byref(rid)))
         self.sizes[rid.value] = (xyz.shape[0], pre.shape[0])
+        return int(rid.value)
+
+    def submit_knn(self, n: int, k: int, density: float, knn_seed: int, horizon: int, params=None, groups=()) -> int:
+        """A request for the network build_knn(n, k, density, knn_seed) describes, built by
+        one of the server's builder threads (no arrays cross the call)."""
+        groups = list(groups)
+        garr = (Group * max(1, len(groups)))()
+        for i, g in enumerate(groups):
+            garr[i] = Group(int(g["first"]), int(g["count"]), float(g["rate_hz"]), int(g.get("correlated", 1)),
+                            int(g.get("jitter", 2)))
+        p = params or default_params()
+        rid = ctypes.c_int64()
+        _check(self._lib.nc_server_submit_knn(self._h, int(n), int(k), float(density), int(knn_seed), ctypes.byref(p),
+                                              len(groups), ctypes.cast(garr, ctypes.c_void_p), int(horizon),
+                                              ctypes.byref(rid)))
+        self.sizes[rid.value] = (int(n), int(n) * int(k))
         return int(rid.value)
 
     def poll(self, capacity: int = 4096):

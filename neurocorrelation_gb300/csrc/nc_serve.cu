@@ -84,6 +84,12 @@ private:
 struct Request {
     int64_t id = 0;
     nc_net_spec spec{};
+    // a kNN network described by its parameters (nc_server_submit_knn): built by the
+    // builder thread, which holds its arrays only while it prepares the request
+    bool knn = false;
+    int32_t knn_k = 0;
+    float knn_density = 0.0f;
+    uint64_t knn_seed = 0;
     std::vector<float> xyz, weight, length;
     std::vector<int32_t> from, to;
     std::vector<uint8_t> inh;
@@ -110,6 +116,9 @@ struct Kept {
 };
 
 constexpr int kGroupsPerNet = 16;
+constexpr int64_t kBuiltHostCap = 8ll << 30;
+// host bytes of a prepared request's tables (CSC, CSR, weights, maps)
+int64_t host_bytes(const nc::NetHost& h) { return h.s * 64 + (int64_t)h.n * 64; }
 // per synapse: w t_arr term inh | out_* last_arr (event form) or csc_pre csc_dl la_c (dense)
 constexpr double kSynBytesEvent = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 4 + 0.125;
 constexpr double kSynBytesDense = 4 + 4 + 8 + 4 + 4 + 2 + 4 + 0.125 + 0.125;  // + csc_post, window bit
@@ -142,6 +151,9 @@ struct nc_server {
     int64_t next_id = 1;
     std::deque<std::unique_ptr<Request>> todo;              // awaiting a builder
     std::map<int64_t, std::unique_ptr<Resident>> built;     // prepared, awaiting admission
+    // host memory the prepared, unadmitted requests hold; builders pause above
+    // kBuiltHostCap so that a burst of submissions cannot fill the host
+    int64_t built_host_bytes = 0;
     std::vector<nc_request_done> finished;                  // not yet polled
     std::map<int64_t, Kept> kept;
     nc_server_stats st{};
@@ -352,7 +364,7 @@ void nc_server::builder_loop()
         std::unique_ptr<Request> rq;
         {
             std::unique_lock<std::mutex> lk(mu);
-            cv.wait(lk, [&] { return stop || !todo.empty(); });
+            cv.wait(lk, [&] { return stop || (!todo.empty() && built_host_bytes < kBuiltHostCap); });
             if (stop && todo.empty()) return;
             rq = std::move(todo.front());
             todo.pop_front();
@@ -361,11 +373,31 @@ void nc_server::builder_loop()
         r->id = rq->id;
         r->submit_s = rq->submit_s;
         r->horizon = rq->spec.horizon;
-        const nc_net_spec& sp = rq->spec;
+        nc_net_spec& sp = rq->spec;
         std::string err;
-        int rc = nc::build_net(sp.n_neurons, rq->xyz.empty() ? nullptr : rq->xyz.data(), sp.n_synapses, rq->from.data(),
-                               rq->to.data(), rq->weight.data(), rq->length.empty() ? nullptr : rq->length.data(),
-                               rq->inh.empty() ? nullptr : rq->inh.data(), sp.params, r->host, err);
+        int rc = NC_OK;
+        if (rq->knn) {
+            const size_t n = (size_t)sp.n_neurons, m = n * (size_t)rq->knn_k;
+            rq->xyz.resize(3 * n);
+            rq->from.resize(m);
+            rq->to.resize(m);
+            rq->weight.resize(m);
+            rc = nc_build_knn(sp.n_neurons, rq->knn_k, rq->knn_density, rq->knn_seed, rq->xyz.data(), rq->from.data(),
+                              rq->to.data(), rq->weight.data());
+            if (rc != NC_OK) err = "bad kNN request";
+            sp.n_synapses = (int64_t)m;
+        }
+        if (rc == NC_OK)
+            rc = nc::build_net(sp.n_neurons, rq->xyz.empty() ? nullptr : rq->xyz.data(), sp.n_synapses,
+                               rq->from.data(), rq->to.data(), rq->weight.data(),
+                               rq->length.empty() ? nullptr : rq->length.data(), rq->inh.empty() ? nullptr : rq->inh.data(),
+                               sp.params, r->host, err);
+        if (rq->knn) {  // the arrays are not needed past the host layout
+            std::vector<float>().swap(rq->xyz);
+            std::vector<int32_t>().swap(rq->from);
+            std::vector<int32_t>().swap(rq->to);
+            std::vector<float>().swap(rq->weight);
+        }
         if (rc == NC_OK) rc = nc::set_groups(r->host, (int32_t)rq->groups.size(), rq->groups.data(), err);
         if (rc == NC_OK && (int)r->host.groups.size() > kGroupsPerNet) {
             rc = NC_ERR_INVALID;
@@ -387,6 +419,7 @@ void nc_server::builder_loop()
         r->err = err;
         {
             std::lock_guard<std::mutex> lk(mu);
+            built_host_bytes += host_bytes(r->host);
             built.emplace(r->id, std::move(r));
         }
         cv.notify_all();
@@ -573,6 +606,7 @@ void nc_server::scheduler_loop()
             for (auto it = built.begin(); it != built.end();) {
                 Resident& r = *it->second;
                 if (r.status != NC_OK) {
+                    built_host_bytes -= host_bytes(r.host);
                     rejected.push_back(std::move(it->second));
                     it = built.erase(it);
                     continue;
@@ -582,6 +616,7 @@ void nc_server::scheduler_loop()
                     ++it;
                     continue;
                 }
+                built_host_bytes -= host_bytes(r.host);
                 if (rc != NC_OK) {
                     r.status = rc;
                     r.err = err;
@@ -613,6 +648,7 @@ void nc_server::scheduler_loop()
             }
         }
         if (!rejected.empty()) cv_done.notify_all();
+        if (changed || !rejected.empty()) cv.notify_all();  // builders paused on the host cap
         if (changed && upload_tiles(err) != NC_OK) return;
         if (active.empty()) continue;
         // one batch of G launch pairs over every resident network
@@ -742,6 +778,36 @@ int nc_server_submit(nc_server* s, const nc_net_spec* sp, int64_t* request_id)
     if (sp->syn_length) rq->length.assign(sp->syn_length, sp->syn_length + m);
     if (sp->syn_inhibitory) rq->inh.assign(sp->syn_inhibitory, sp->syn_inhibitory + m);
     if (sp->n_groups) rq->groups.assign(sp->groups, sp->groups + sp->n_groups);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        rq->id = s->next_id++;
+        rq->submit_s = s->now();
+        *request_id = rq->id;
+        s->todo.push_back(std::move(rq));
+        s->st.submitted++;
+        s->outstanding++;
+    }
+    s->cv.notify_all();
+    return NC_OK;
+}
+
+int nc_server_submit_knn(nc_server* s, int32_t n, int32_t k, float density, uint64_t knn_seed,
+                         const nc_params* params, int32_t n_groups, const nc_group* groups, int32_t horizon,
+                         int64_t* request_id)
+{
+    if (!s || !params || !request_id) return sfail(NC_ERR_INVALID, "null argument");
+    if (n < 2 || k < 1 || k >= n || !(density > 0.0f) || horizon < 0 || n_groups < 0 || (n_groups > 0 && !groups))
+        return sfail(NC_ERR_INVALID, "bad kNN request (need 1 <= k < n, density > 0)");
+    auto rq = std::make_unique<Request>();
+    rq->knn = true;
+    rq->knn_k = k;
+    rq->knn_density = density;
+    rq->knn_seed = knn_seed;
+    rq->spec.n_neurons = n;
+    rq->spec.params = *params;
+    rq->spec.horizon = horizon;
+    rq->spec.n_groups = n_groups;
+    if (n_groups) rq->groups.assign(groups, groups + n_groups);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         rq->id = s->next_id++;

@@ -65,3 +65,35 @@ def test_served_rejects_request_over_budget(nc):
     done = srv.poll()
     assert len(done) == 1 and done[0]["request_id"] == rid and done[0]["status"] == -7
     srv.close()
+
+
+def test_served_knn_requests_equal_alone(nc, oracle_mod):
+    """Requests sent as kNN parameters (nc_server_submit_knn), built on the server's
+    builder threads, mixed with requests sent as arrays: each equals the oracle run on the
+    network the oracle's own kNN restatement builds."""
+    G, O = nc, oracle_mod
+    srv = G.Server(budget_bytes=512 << 20, max_networks=4, steps_per_batch=16, build_threads=3, keep_results=True)
+    knn = [(1500, 20, 11, 240), (700, 40, 12, 180), (3000, 12, 13, 300), (900, 30, 14, 150)]
+    groups = [dict(first=0, count=10, rate_hz=30.0, correlated=1, jitter=2)]
+    ids = []
+    for q, (n, k, seed, horizon) in enumerate(knn):
+        p = G.default_params(seed=500 + q)
+        ids.append(srv.submit_knn(n, k, 8.0, seed, horizon, params=p, groups=groups))
+        if q == 1:
+            xyz, pre, post, w = knn_net(300, 10, 77)
+            ids.append(srv.submit(dict(xyz=xyz, pre=pre, post=post, weight=w, params=G.default_params(seed=99),
+                                       groups=groups, horizon=200)))
+    srv.drain()
+    done = {d["request_id"]: d for d in srv.poll()}
+    assert sorted(done) == sorted(ids)
+    k_ids = [i for q, i in enumerate(ids) if q != 2]
+    for rid, (n, k, seed, horizon), q in zip(k_ids, knn, range(len(knn))):
+        d = done[rid]
+        assert d["status"] == 0 and d["steps"] == horizon and d["n_synapses"] == n * k
+        w, pot = srv.fetch(rid)
+        xyz, pre, post, wk = O.build_knn(n, k, 8.0, seed)
+        o = O.OracleS(xyz, pre, post, wk, params=O.default_params(seed=500 + q), groups=groups)
+        o.run(horizon)
+        np.testing.assert_array_equal(w.view(np.uint32), o.weights().view(np.uint32))
+        np.testing.assert_array_equal(pot.view(np.uint32), o.potentials().view(np.uint32))
+    srv.close()
