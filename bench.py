@@ -277,16 +277,20 @@ def c4_requests(n_req, horizon_scale, seed=4):
     return reqs
 
 
-def one_at_a_time(G, nets, mode, arrivals=None):
+def one_at_a_time(G, nets, mode, arrivals=None, device_build=False):
     """The plain drop-in, one network after another: create, run the horizon, read the
     counters, destroy.  Returns (events, busy seconds, run-only seconds, per-request
     latency or None); run-only leaves out building and uploading each network."""
     events, busy, run_s, clock, lat = 0, 0.0, 0.0, 0.0, []
     for q, d in enumerate(nets):
         t0 = time.perf_counter()
-        if "knn" in d:  # the drop-in's own kNN construction (on the device in the dense form)
+        if "knn" in d and device_build:  # the drop-in's device kNN builder (dense form)
             n, k, kseed = d["knn"]
             net = G.NeuCor.knn(n, k, 8.0, seed=kseed, params=G.default_params(seed=d["seed"], step_mode=mode))
+        elif "knn" in d:  # built on the host, as the server's builder threads do
+            n, k, kseed = d["knn"]
+            xyz, pre, post, w = G.build_knn(n, k, 8.0, seed=kseed)
+            net = G.NeuCor.from_arrays(xyz, pre, post, w, params=G.default_params(seed=d["seed"], step_mode=mode))
         else:
             net = G.NeuCor.from_arrays(d["xyz"], d["pre"], d["post"], d["weight"],
                                        params=G.default_params(seed=d["seed"], step_mode=mode))
@@ -364,14 +368,19 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
     span = max(d["done_s"] for d in ok) - min(d["submit_s"] for d in ok)
     events = sum(d["launched"] for d in ok)
     t_one = time.perf_counter()
-    ev1, busy1, _, lat1 = one_at_a_time(G, reqs, mode, arrivals=[r["arrival"] for r in reqs])
-    span1 = max(a + l for a, l in zip([r["arrival"] for r in reqs], lat1)) - reqs[0]["arrival"]
+    arr = [r["arrival"] for r in reqs]
+    ev1, busy1, _, lat1 = one_at_a_time(G, reqs, mode, arrivals=arr)
+    span1 = max(a + l for a, l in zip(arr, lat1)) - reqs[0]["arrival"]
+    t_dev = time.perf_counter()
+    ev2, _, _, lat2 = one_at_a_time(G, reqs, mode, arrivals=arr, device_build=True)
+    span2 = max(a + l for a, l in zip(arr, lat2)) - reqs[0]["arrival"]
     t_end = time.perf_counter()
     return {"workload": f"{n_req} requests, Poisson arrivals at 50/s, 500-200k neurons, fan-out 20-150, "
                         f"horizons log-uniform 1k-100k steps x {horizon_scale}, 1-8 input groups each; "
-                        "served: each sent as kNN parameters and built by the server's builder threads; "
-                        "one at a time: each built by the drop-in's device kNN builder, run and read back",
-            "wall_s": {"served": t_one - t0, "one_at_a_time": t_end - t_one},
+                        "served: each sent as kNN parameters and built on the host by the server's builder "
+                        "threads; one at a time: each built on the host (as the server does), run and read "
+                        "back; and again with the drop-in's device kNN builder",
+            "wall_s": {"served": t_one - t0, "one_at_a_time": t_dev - t_one, "one_at_a_time_device_build": t_end - t_dev},
             "requests": n_req, "finished": len(ok), "horizon_scale": horizon_scale, "arrival_rate_per_s": 50,
             "budget_gb": budget / 1e9, "events_per_s": events / span, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "peak_resident_networks": sst["peak_resident_networks"],
@@ -379,7 +388,11 @@ def measure_served(G, n_req, horizon_scale, budget, mode):
             "one_at_a_time_events_per_s": ev1 / span1,
             "one_at_a_time_p50_latency_s": float(np.percentile(lat1, 50)),
             "one_at_a_time_p99_latency_s": float(np.percentile(lat1, 99)),
-            "speedup_vs_one_at_a_time": (events / span) / (ev1 / span1)}
+            "speedup_vs_one_at_a_time": (events / span) / (ev1 / span1),
+            "one_at_a_time_device_build_events_per_s": ev2 / span2,
+            "one_at_a_time_device_build_p50_latency_s": float(np.percentile(lat2, 50)),
+            "one_at_a_time_device_build_p99_latency_s": float(np.percentile(lat2, 99)),
+            "speedup_vs_one_at_a_time_device_build": (events / span) / (ev2 / span2)}
 
 
 def measure_large(G, mode, sim_steps=100, timed=5):
