@@ -228,6 +228,14 @@ __device__ int stage_unit(const NcPools& P, int sp, int half, bool flush, StageB
     return 1;
 }
 
+#ifndef NC_FULL_UNIT
+#define NC_FULL_UNIT 1
+#endif
+template <bool B>
+struct BoolTag {
+    static constexpr bool value = B;
+};
+
 // All lanes: bounded wait for the phase of *bar.
 __device__ __forceinline__ bool stage_wait(unsigned long long* bar, uint32_t phase)
 {
@@ -370,6 +378,10 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                 const uint32_t* inh_u = P.inh + (ubase >> 5);
                 const int32_t qoff = half * kUnitSyn;  // the unit's first synapse, relative to the span
                 const int32_t prev_c = C.t - 1;
+                // the chunks of the unit; a full unit (all but a net's last) is compiled
+                // without the per-lane bounds tests
+                auto chunks = [&](auto all_tag) {
+                constexpr bool kAll = decltype(all_tag)::value;
                 for (int h = 0; h < kUnitChunks; h += kStageUnroll) {
                     uint32_t fword[kStageUnroll], ihw[kStageUnroll];
                     float pstv[kStageUnroll];
@@ -379,7 +391,7 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         fword[u] = 0u;
                         pstv[u] = 0.0f;
                         ihw[u] = 0u;
-                        if (q < u_rem) {
+                        if (kAll || q < u_rem) {
                             fword[u] = C.fprev[B.pre[q] >> 5];
                             pstv[u] = C.pst[B.post[q]];
                             ihw[u] = __ldg(inh_u + h + u);
@@ -388,7 +400,7 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
     #pragma unroll
                     for (int u = 0; u < kStageUnroll; ++u) {
                         const int q = (h + u) * 32 + lane;
-                        const bool in = q < u_rem;
+                        const bool in = kAll || q < u_rem;
                         const int32_t la = B.la[q];
                         int32_t lac = in ? la : NC_NEVER;
                         bool launch = false;
@@ -432,7 +444,7 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         // arrivals wrap past KC)
                         const bool win = (uint32_t)prev_c - (uint32_t)lac < (uint32_t)C.kc;
                         const uint32_t wm = __ballot_sync(kFull, win);
-                        if (lane == 0 && (h + u) * 32 < u_rem) win_u[h + u] = wm;
+                        if (lane == 0 && (kAll || (h + u) * 32 < u_rem)) win_u[h + u] = wm;
                         const uint32_t lm = __ballot_sync(kFull, launch);
                         if (lm) {
                             if (launch) {
@@ -455,6 +467,9 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         }
                     }
                 }
+                };
+                if (NC_FULL_UNIT && u_rem == kUnitSyn) chunks(BoolTag<true>{});
+                else chunks(BoolTag<false>{});
                 // the queue holds offsets into this span: drain it before the warp moves on
                 // to another span (the span's next unit follows when it was issued)
                 const bool more = half + 1 < kUnitsPerSpan && ((bits >> ((k + 1) % kStages)) & 1);
