@@ -403,41 +403,38 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         const bool in = kAll || q < u_rem;
                         const int32_t la = B.la[q];
                         int32_t lac = in ? la : NC_NEVER;
-                        bool launch = false;
+                        bool launch = false, srcf = false;
                         float x = 0.0f;
                         if (in) {
                             const uint32_t dl = B.dl[q];
                             // target fired at prev: the sign of its post state
                             const bool tf = __float_as_uint(pstv[u]) == 0x80000000u;
-                            const bool srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
+                            srcf = (fword[u] >> (B.pre[q] & 31)) & 1u;
                             const bool arrived = la == prev_c;
                             const int32_t after = (int32_t)((dl >> 14) & 1u);
                             // free: never launched (NC_NEVER is INT32_MIN, far below) or
                             // prev - la >= KC + after
                             launch = srcf && la + C.kc + after <= prev_c;
-                            nl += launch;
-                            nd += srcf && !launch;
                             const bool ih = (ihw[u] >> lane) & 1u;
                             const float lo = ih ? -1.0f : 0.0f, hi = ih ? 0.0f : 1.0f;
                             const float w0 = B.w[q];
                             float w1 = w0;
                             if (tf) w1 = plasticity_b(w0, lo, hi, trace_at_u(C.tab_pre, C.tab_pre_len, prev_c, B.ta[q]),
                                                       0.0f, C.R);
-                            if (launch) {
-                                // target below the source in caller order and fired at prev:
-                                // its update ran first, post-spike plasticity included
-                                const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
-                                // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                                x = C.dt * (C.c52 * cap);
-                                lac = prev_c + (int32_t)(dl & 0x3fffu);
-                                la_u[q] = lac;
-                            }
-                            float w2 = w1;
-                            if (arrived) {
-                                // the target's post trace at prev (0 when it fired at prev)
-                                w2 = plasticity_b(w1, lo, hi, 0.0f, fabsf(pstv[u]), C.R);
-                                ta_u[q] = prev_c;
-                            }
+                            // the launch's values and the arrival's update are formed in
+                            // every lane and kept by selects and predicated stores
+                            // target below the source in caller order and fired at prev:
+                            // its update ran first, post-spike plasticity included
+                            const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
+                            // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                            x = C.dt * (C.c52 * cap);
+                            const int32_t lnew = prev_c + (int32_t)(dl & 0x3fffu);
+                            if (launch) la_u[q] = lnew;
+                            lac = launch ? lnew : la;
+                            // the target's post trace at prev (0 when it fired at prev)
+                            const float w2a = plasticity_b(w1, lo, hi, 0.0f, fabsf(pstv[u]), C.R);
+                            const float w2 = arrived ? w2a : w1;
+                            if (arrived) ta_u[q] = prev_c;
                             if (tf || arrived) w_u[q] = w2;
                         }
                         // arrived t-KC .. t-1: in the fold of step t (NC_NEVER and later
@@ -446,13 +443,15 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         const uint32_t wm = __ballot_sync(kFull, win);
                         if (lane == 0 && (kAll || (h + u) * 32 < u_rem)) win_u[h + u] = wm;
                         const uint32_t lm = __ballot_sync(kFull, launch);
+                        // launched and dropped, counted once per warp
+                        const int nlm = __popc(lm);
+                        nl += nlm;
+                        nd += __popc(__ballot_sync(kFull, srcf)) - nlm;
                         if (lm) {
-                            if (launch) {
-                                const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                                ws.qs[pos] = qoff + q;
-                                ws.qx[pos] = x;
-                            }
-                            qn += __popc(lm);
+                            const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                            if (launch) ws.qs[pos] = qoff + q;
+                            if (launch) ws.qx[pos] = x;
+                            qn += nlm;
                             if (qn >= 32) {
                                 __syncwarp();
                                 P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], C.e_term);
@@ -477,8 +476,8 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                     __syncwarp();
                     if (lane < qn) P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], C.e_term);
                     qn = 0;
-                    acc[0] += (unsigned long long)warp_sum(nl);
-                    acc[1] += (unsigned long long)warp_sum(nd);
+                    acc[0] += (unsigned long long)nl;
+                    acc[1] += (unsigned long long)nd;
                     nl = nd = 0;
                 }
             }

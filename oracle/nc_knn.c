@@ -1,6 +1,6 @@
 /* nc_knn.c — the workloads' k-nearest-neighbour networks, restated on the CPU.
  *
- * TEST INFRASTRUCTURE (the checker, with nc_oracle.c): builds the same network as the
+ * TEST INFRASTRUCTURE (part of the oracle, with nc_oracle.c): builds the same network as the
  * library's nc_build_knn / nc_create_knn from the definition alone, so that fixtures,
  * the CPU baseline and the reference arm of the benchmark can make the workloads'
  * networks without loading the library under test.

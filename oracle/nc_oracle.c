@@ -2,7 +2,7 @@
  * Oracle-S — CPU restatement of the NeuCor simulation step (TEST INFRASTRUCTURE).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
- * arm load this file's library.  It is the checker, never the product.
+ * arm load this file's library.  It is the oracle, never the product.
  *
  * Every function below names the reference lines it restates.  Arithmetic is
  * kept in the reference's own types: float state, double where the reference

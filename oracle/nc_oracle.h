@@ -1,6 +1,6 @@
 /*
  * Oracle-S: the CPU restatement of NeuroCorrelation's simulation step, used as
- * TEST INFRASTRUCTURE ONLY (the parity checker for the CUDA path and the timed
+ * TEST INFRASTRUCTURE ONLY (the parity oracle for the CUDA path and the timed
  * CPU port in bench.py).  Nothing in the shipped library links or calls it.
  *
  * It follows the reference's per-object code in src/NeuCor.cpp expression by

@@ -2,7 +2,7 @@
 
 * ``OracleS``  — ctypes wrapper of ``liboracle_s.so`` (nc_oracle.c), the stepped CPU
   restatement of the NeuCor step.  Used by tests/, ``__graft_entry__.smoke()`` and
-  bench.py's CPU baseline as the checker; never by the product.
+  bench.py's CPU baseline as the oracle; never by the product.
 * ``run_reference`` — runs ``_ref/neucor_ref`` (the reference's own src/NeuCor.cpp
   compiled from its sources by oracle/Makefile) on a scenario.  Only available where
   the reference tree was present at build time.

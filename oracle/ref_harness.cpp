@@ -140,7 +140,7 @@ static Scenario read_scenario(const char* path)
     return sc;
 }
 
-// ------------------------------------------------------------------ driver
+// ------------------------------------------------------------------ harness
 class NeuCor_Renderer;
 struct NeuCor_Lengths {
     static void collect(NeuCor& brain, std::vector<float>& out);

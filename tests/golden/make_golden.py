@@ -76,8 +76,8 @@ def c1_stats(mode, seed, steps=10000, window=1000):
 
 def c1_statistics():
     """F. C1 for its 10,000 steps through the reference's own NeuCor::run.
-    native: runAll, synapse lengths on the step grid (the benchmark spec's whole-step
-    delays), background fire times on the step grid; three simulation seeds.
+    native: runAll, synapse lengths on the step grid (whole-step delays, as in the
+    stepped model), background fire times on the step grid; three simulation seeds.
     continuous: the unmodified timing (lengths as built, glibc rand() background at
     random times inside the step); one seed.
     continuous_grid: as continuous with the lengths on the step grid (only the

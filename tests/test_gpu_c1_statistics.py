@@ -5,7 +5,7 @@ a correlated and an uncorrelated group of 10 inputs at 20 Hz, STDP on) for its f
 
 The reference ran unmodified (src/NeuCor.cpp compiled from its sources, driven by
 oracle/ref_harness.cpp; tests/golden/make_golden.py, section c1_stats) with every event
-on the step grid: runAll, synapse lengths of whole-step delays (the benchmark spec's integer
+on the step grid: runAll, synapse lengths of whole-step delays (the stepped model's integer
 delays) and background fire times on the step boundary.  Its per-window population
 rates and final weights are the fixture.  The GPU and the reference compute the same
 bits until the first same-step order coincidence, then diverge as chaotic trajectories
