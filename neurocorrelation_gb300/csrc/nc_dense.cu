@@ -421,20 +421,21 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                             float w1 = w0;
                             if (tf) w1 = plasticity_b(w0, lo, hi, trace_at_u(C.tab_pre, C.tab_pre_len, prev_c, B.ta[q]),
                                                       0.0f, C.R);
-                            // the launch's values and the arrival's update are formed in
-                            // every lane and kept by selects and predicated stores
-                            // target below the source in caller order and fired at prev:
-                            // its update ran first, post-spike plasticity included
-                            const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
-                            // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
-                            x = C.dt * (C.c52 * cap);
-                            const int32_t lnew = prev_c + (int32_t)(dl & 0x3fffu);
-                            if (launch) la_u[q] = lnew;
-                            lac = launch ? lnew : la;
-                            // the target's post trace at prev (0 when it fired at prev)
-                            const float w2a = plasticity_b(w1, lo, hi, 0.0f, fabsf(pstv[u]), C.R);
-                            const float w2 = arrived ? w2a : w1;
-                            if (arrived) ta_u[q] = prev_c;
+                            if (launch) {
+                                // target below the source in caller order and fired at prev:
+                                // its update ran first, post-spike plasticity included
+                                const float cap = (((dl >> 15) & 1u) && tf) ? w1 : w0;
+                                // AP_depolFac = 0.2f; *= 52.0; *= weight  (src/NeuCor.cpp:729-731)
+                                x = C.dt * (C.c52 * cap);
+                                lac = prev_c + (int32_t)(dl & 0x3fffu);
+                                la_u[q] = lac;
+                            }
+                            float w2 = w1;
+                            if (arrived) {
+                                // the target's post trace at prev (0 when it fired at prev)
+                                w2 = plasticity_b(w1, lo, hi, 0.0f, fabsf(pstv[u]), C.R);
+                                ta_u[q] = prev_c;
+                            }
                             if (tf || arrived) w_u[q] = w2;
                         }
                         // arrived t-KC .. t-1: in the fold of step t (NC_NEVER and later
@@ -448,10 +449,12 @@ __device__ __forceinline__ void synapse_pass(const NcPools& P, WarpStage& ws, Pa
                         nl += nlm;
                         nd += __popc(__ballot_sync(kFull, srcf)) - nlm;
                         if (lm) {
-                            const int pos = qn + __popc(lm & ((1u << lane) - 1u));
-                            if (launch) ws.qs[pos] = qoff + q;
-                            if (launch) ws.qx[pos] = x;
-                            qn += nlm;
+                            if (launch) {
+                                const int pos = qn + __popc(lm & ((1u << lane) - 1u));
+                                ws.qs[pos] = qoff + q;
+                                ws.qx[pos] = x;
+                            }
+                            qn += __popc(lm);
                             if (qn >= 32) {
                                 __syncwarp();
                                 P.term[s_span + ws.qs[lane]] = make_term(ws.qx[lane], C.e_term);
