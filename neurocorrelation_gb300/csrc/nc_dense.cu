@@ -522,11 +522,20 @@ __global__ void __launch_bounds__(32 * kStageWarps, NC_STAGE_MIN_BLOCKS) k_dense
 // window bits are read 256 synapses (8 words) at a time and streamed in batches of 8
 // across word boundaries, so that a warp's batch count is its busiest lane's, not a sum
 // of per-word maxima.
+//
+// When no term of the net can be negative (nonneg_terms), the running sum only grows
+// (each `float += double` rounds a larger value, and rounding keeps the order), and so
+// does charge_passive's result.  Once that result crosses the threshold the neuron fires
+// whatever the remaining terms are, and its potential is then replaced by the AP table
+// (src/NeuCor.cpp:682-686, 706-714): the fold stops there and returns the partial sum,
+// which leads the update to the same decision.
 __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, int32_t j, float pot)
 {
     const int64_t s0 = P.in_ptr[D.ptr_base + j];
     const int64_t s1 = P.in_ptr[D.ptr_base + j + 1];
     if (s1 <= s0) return pot;
+    const bool stop = NC_FOLD_EARLY_EXIT && D.nonneg_terms;
+    const float leak = D.leak;
     double pd = (double)pot;
     const int64_t wa0 = s0 >> 5, wa1 = (s1 - 1) >> 5;
     for (int64_t wb = wa0; wb <= wa1; wb += 8) {
@@ -564,6 +573,8 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
             for (int k = 0; k < 8; ++k)
                 if (b[k] >= 0) v[k] = tp[b[k]];
             pd = fold8(pd, v, b, tp);
+            // pd holds a float value exactly
+            if (stop && fires_at((float)pd, leak)) return (float)pd;
         }
     }
     return __double2float_rn(pd);
@@ -619,6 +630,10 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
                 const int32_t lf = P.lf[D.neuron_base + j];
                 need = !(lf != NC_NEVER && t - lf < D.kc) &&
                        P.in_ptr[D.ptr_base + j + 1] > P.in_ptr[D.ptr_base + j];
+                // with no negative term, a neuron already over the threshold fires whatever
+                // its sum (see fold_row)
+                if (NC_FOLD_EARLY_EXIT && need && D.nonneg_terms && fires_at(P.pot[D.neuron_base + j], D.leak))
+                    need = false;
                 if (NC_NEURON_EARLY) {
                     const int32_t pj = D.neuron_base + j;
                     const int32_t cid = D.permuted ? P.orig_id[pj] : j;

@@ -112,6 +112,20 @@ static __device__ __noinline__ double fold_exact8(double pd, const double* tp, i
     return pd;
 }
 
+// Whether a neuron out of its AP with potential `pot` (its sum so far) fires:
+// charge_passive and the threshold test of charge_thresholdCheck (src/NeuCor.cpp:677-686),
+// with the step kernels' own operations.  When no term of the net can be negative the sum
+// only grows (rounding keeps the order) and so does this result, so a fold may stop once
+// it holds: the neuron fires whatever the remaining terms are, and its potential is then
+// replaced by the AP table (src/NeuCor.cpp:706-714).
+#ifndef NC_FOLD_EARLY_EXIT
+#define NC_FOLD_EARLY_EXIT 1
+#endif
+static __device__ __forceinline__ bool fires_at(float pot, float leak)
+{
+    return -55.0f < (pot - -70.0f) * leak + -70.0f;
+}
+
 // Folds v[k] = tp[b[k]] for every k with b[k] >= 0 (ascending) into pd, the float
 // accumulator held as a double: `potential += term`, one double add and an integer
 // rounding to float per term.  (A fold on float arithmetic alone — the term split into

@@ -89,6 +89,8 @@ struct NcNetDesc {
     unsigned long long* stats; // 4 counters: fires, launched, dropped, steps
     int64_t n_syn;        // synapses (the pool range is padded to a multiple of 32)
     float tsum;           // NeuCor::currentTime after t-1 steps: the float sum of t-1 runSpeeds
+    int32_t nonneg_terms; // 1: no launch can add a negative term (no inhibitory synapse, no
+                          // negative weight), so a neuron's sum only grows within a step
 };
 
 struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8 chunks of

@@ -314,6 +314,13 @@ int build_net(int32_t n, const float* xyz, int64_t n_syn, const int32_t* from, c
         }
     }
 
+    // Every term a launch can add is >= 0 when no synapse is inhibitory and no weight is
+    // negative: plasticity keeps an excitatory weight in [0, 1] (src/NeuCor.cpp:757-761)
+    // and no call changes a weight after creation.
+    h.nonneg_terms = true;
+    for (uint32_t b : h.inh_bits) h.nonneg_terms = h.nonneg_terms && b == 0u;
+    for (float x : h.w) h.nonneg_terms = h.nonneg_terms && x >= 0.0f;
+
     // tables: presynaptic trace, postsynaptic trace, AP shape
     h.tables.clear();
     if (!trace_table(p.presynaptic_trace_decay, h.dt, h.tables, h.tab_pre_len) ||

@@ -45,6 +45,7 @@ struct NetHost {
     std::vector<float> tables;              // pre trace | post trace | AP shape
     int32_t tab_pre_len = 0, tab_post_len = 0, ap_len = 0;
     std::vector<NcGroupDev> groups;
+    bool nonneg_terms = true;               // no inhibitory synapse and no negative weight
 
     int64_t device_bytes() const;
 };

@@ -179,6 +179,10 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                 const bool in_ap = lf != NC_NEVER && t - lf < D.kc;
                 if (r1 > r0) {
                     double pd = (double)pot;
+                    // the sum is not needed inside the AP, nor, when no term can be
+                    // negative, once the neuron is certain to fire (fires_at)
+                    const bool stop = NC_FOLD_EARLY_EXIT && D.nonneg_terms;
+                    bool settled = in_ap || (stop && fires_at(pot, D.leak));
                     uint32_t* ring = P.ring + D.ring_base;
                     const int64_t rw = D.ring_words;
                     const int32_t kc = D.kc;
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             olo = x;  // ends as the word of slot t-KC when t-KC >= 1
                             ohi = y;
                         }
-                        unsigned long long bits = in_ap ? 0ull : (lo | ((unsigned long long)hi << 32));
+                        unsigned long long bits = settled ? 0ull : (lo | ((unsigned long long)hi << 32));
                         const unsigned long long arr = stdp ? (alo | ((unsigned long long)ahi << 32)) : 0ull;
                         const int64_t sb = s0 + (int64_t)(wi - r0) * 32;
                         unsigned long long ih = 0ull;
@@ -231,6 +235,10 @@ __global__ void __launch_bounds__(256, NC_NEURON_MIN_BLOCKS) k_neuron_step(NcPoo
                             for (int k = 0; k < 8; ++k)
                                 if (b[k] >= 0) v[k] = tp[b[k]];
                             pd = fold8(pd, v, b, tp);
+                            if (stop && fires_at((float)pd, D.leak)) {
+                                settled = true;
+                                bits = 0ull;
+                            }
                         }
                         // the spikes that arrived KC steps ago are released (AP_fireTime = 0)
                         if (oldest >= 1) {

@@ -148,6 +148,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         d.n_groups = (int32_t)std::min<size_t>(h.groups.size(), (size_t)ngroups_each);
         d.active = 1;
         d.permuted = h.permuted ? 1 : 0;
+        d.nonneg_terms = h.nonneg_terms ? 1 : 0;
         d.dt = h.dt;
         d.leak = h.leak;
         d.c52 = h.c52;

@@ -521,6 +521,7 @@ int nc_server::admit(Resident& r, std::string& err)
     d.n_groups = (int32_t)h.groups.size();
     d.active = 1;
     d.permuted = h.permuted ? 1 : 0;
+    d.nonneg_terms = h.nonneg_terms ? 1 : 0;
     d.dt = h.dt;
     d.leak = h.leak;
     d.c52 = h.c52;
