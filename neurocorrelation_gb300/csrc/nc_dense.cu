@@ -599,6 +599,10 @@ __device__ __forceinline__ float fold_row(const NcPools& P, const NcNetDesc& D, 
 #define NC_NEURON_EARLY 1
 #endif
 
+#ifndef NC_FOLD_PACK
+#define NC_FOLD_PACK 1
+#endif
+
 __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
 {
     int* s_net = sh.s_net;
@@ -650,24 +654,32 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
                 }
             }
         }
-        const uint32_t need_m = __ballot_sync(kFull, need);
-        if (lane == 0) s_cnt[wib] = __popc(need_m);
-        __syncthreads();
-        int base = 0, total = 0;
-        for (int w = 0; w < wpb; ++w) {
-            base += w < wib ? s_cnt[w] : 0;
-            total += s_cnt[w];
-        }
-        if (need) s_list[base + __popc(need_m & ((1u << lane) - 1u))] = (uint16_t)(wib * 32 + lane);
-        __syncthreads();
-        for (int r = threadIdx.x; r < total; r += blockDim.x) {
-            const int ent = s_list[r];
-            const NcTile tile = P.tiles[tb * wpb + (ent >> 5)];
+        if (NC_FOLD_PACK) {
+            const uint32_t need_m = __ballot_sync(kFull, need);
+            if (lane == 0) s_cnt[wib] = __popc(need_m);
+            __syncthreads();
+            int base = 0, total = 0;
+            for (int w = 0; w < wpb; ++w) {
+                base += w < wib ? s_cnt[w] : 0;
+                total += s_cnt[w];
+            }
+            if (need) s_list[base + __popc(need_m & ((1u << lane) - 1u))] = (uint16_t)(wib * 32 + lane);
+            __syncthreads();
+            for (int r = threadIdx.x; r < total; r += blockDim.x) {
+                const int ent = s_list[r];
+                const NcTile tile = P.tiles[tb * wpb + (ent >> 5)];
+                const NcNetDesc& D = P.nets[tile.net];
+                const int32_t j = tile.first + (ent & 31);
+                s_pot[ent] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
+            }
+            __syncthreads();
+        } else if (need) {
+            // each lane folds its own neuron (no packing, no block barrier)
+            const NcTile tile = P.tiles[tix];
             const NcNetDesc& D = P.nets[tile.net];
-            const int32_t j = tile.first + (ent & 31);
-            s_pot[ent] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
+            const int32_t j = tile.first + lane;
+            s_pot[wib * 32 + lane] = fold_row(P, D, j, P.pot[D.neuron_base + j]);
         }
-        __syncthreads();
         if (tix >= n_tiles) continue;
         const NcTile tile = P.tiles[tix];
         const NcNetDesc& D = P.nets[tile.net];
