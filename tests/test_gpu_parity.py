@@ -86,6 +86,26 @@ def test_gpu_matches_reference_fixture(nc, name, mode):
     assert abs(net.getTime() - steps * float(fx["p_run_speed"])) < 1e-3
 
 
+def edited_weights(net, edit):
+    xyz, pre, post, w = net
+    w = np.array(w, np.float32)
+    edit(w)
+    return xyz, pre, post, w
+
+
+def zero_weights(w):
+    """Exact zeros and negative zeros among non-negative weights: every term is still >= 0,
+    so the neuron passes may stop a fold once the neuron is certain to fire."""
+    w[::5] = 0.0
+    w[1::10] = -0.0
+
+
+def one_negative(w):
+    """One negative weight among non-negative ones: the net's terms may be negative, so
+    every fold runs to its last term."""
+    w[17] = -0.25
+
+
 SCENARIOS = [
     # (label, network, params, groups, steps)
     ("knn300_inh", lambda: knn_net(300, 10, 21, inhibitory=0.2), dict(seed=31),
@@ -103,6 +123,10 @@ SCENARIOS = [
     ("knn200_nobg_lr", lambda: knn_net(200, 16, 27), dict(seed=37, background_firing=0, learning_rate=2.0,
                                                           presynaptic_factor=0.2, postsynaptic_factor=0.1),
      [dict(first=0, count=40, rate_hz=25.0, correlated=1, jitter=2)], 600),
+    ("knn400_zero_weights", lambda: edited_weights(knn_net(400, 24, 29), zero_weights), dict(seed=39),
+     [dict(first=0, count=30, rate_hz=40.0, correlated=1, jitter=2)], 500),
+    ("knn300_one_negative", lambda: edited_weights(knn_net(300, 12, 30), one_negative), dict(seed=40),
+     [dict(first=10, count=20, rate_hz=40.0, correlated=1, jitter=2)], 400),
 ]
 
 
