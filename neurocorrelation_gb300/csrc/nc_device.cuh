@@ -150,9 +150,14 @@ static __device__ __forceinline__ void philox(uint32_t a, uint32_t b, uint32_t s
     nc_philox(a, b, stream, c, D.key0, D.key1, out);
 }
 
+#ifndef NC_GROUP_RANGE
+#define NC_GROUP_RANGE 1
+#endif
 // Whether input neuron j requests a fire at step t (Poisson groups).
 static __device__ bool input_request(const NcPools& P, const NcNetDesc& D, int32_t j, int32_t t)
 {
+    // most neurons are in no group: one range test instead of a walk over the groups
+    if (NC_GROUP_RANGE && (j < D.group_lo || j >= D.group_hi)) return false;
     uint32_t o[4];
     for (int g = 0; g < D.n_groups; ++g) {
         const NcGroupDev G = P.groups[D.group_base + g];

@@ -91,7 +91,27 @@ struct NcNetDesc {
     float tsum;           // NeuCor::currentTime after t-1 steps: the float sum of t-1 runSpeeds
     int32_t nonneg_terms; // 1: no launch can add a negative term (no inhibitory synapse, no
                           // negative weight), so a neuron's sum only grows within a step
+    int32_t group_lo;     // caller ids [group_lo, group_hi) hold every input group's members
+    int32_t group_hi;
 };
+
+// The smallest id range holding the members of groups g[0..n) (empty when n is 0).
+inline void nc_group_range(const NcGroupDev* g, int n, int32_t& lo, int32_t& hi)
+{
+    lo = 0;
+    hi = 0;
+    for (int k = 0; k < n; ++k) {
+        if (g[k].count <= 0) continue;
+        const int32_t a = g[k].first, b = g[k].first + g[k].count;
+        if (lo == hi) {
+            lo = a;
+            hi = b;
+        } else {
+            lo = a < lo ? a : lo;
+            hi = b > hi ? b : hi;
+        }
+    }
+}
 
 struct NcTile {          // 32 consecutive neurons of one net, or (span table) 8 chunks of
     int32_t net;         // 32 in-synapses

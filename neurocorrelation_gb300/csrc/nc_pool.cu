@@ -146,6 +146,7 @@ int Engine::build(const std::vector<const NetHost*>& nets, int group_capacity, s
         d.ap_base = (int32_t)(tables + h.tab_pre_len + h.tab_post_len);
         d.group_base = sl.group_base;
         d.n_groups = (int32_t)std::min<size_t>(h.groups.size(), (size_t)ngroups_each);
+        nc_group_range(h.groups.data(), d.n_groups, d.group_lo, d.group_hi);
         d.active = 1;
         d.permuted = h.permuted ? 1 : 0;
         d.nonneg_terms = h.nonneg_terms ? 1 : 0;
@@ -519,6 +520,11 @@ int Engine::set_groups(int net, const std::vector<NcGroupDev>& groups, std::stri
         NC_CK(cudaMemcpyAsync(P.groups + slots[net].group_base, groups.data(), groups.size() * sizeof(NcGroupDev),
                               cudaMemcpyHostToDevice, stream));
     const int32_t ng = (int32_t)groups.size();
+    int32_t range[2];
+    nc_group_range(groups.data(), ng, range[0], range[1]);
+    static_assert(offsetof(NcNetDesc, group_hi) == offsetof(NcNetDesc, group_lo) + sizeof(int32_t), "range");
+    NC_CK(cudaMemcpyAsync((char*)(P.nets + net) + offsetof(NcNetDesc, group_lo), range, sizeof(range),
+                          cudaMemcpyHostToDevice, stream));
     NC_CK(put_field(P.nets, net, offsetof(NcNetDesc, n_groups), ng, stream));
     NC_CK(cudaStreamSynchronize(stream));
     return NC_OK;

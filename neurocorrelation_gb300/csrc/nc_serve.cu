@@ -519,6 +519,7 @@ int nc_server::admit(Resident& r, std::string& err)
     d.ap_base = (int32_t)(tb + h.tab_pre_len + h.tab_post_len);
     d.group_base = r.slot * kGroupsPerNet;
     d.n_groups = (int32_t)h.groups.size();
+    nc_group_range(h.groups.data(), d.n_groups, d.group_lo, d.group_hi);
     d.active = 1;
     d.permuted = h.permuted ? 1 : 0;
     d.nonneg_terms = h.nonneg_terms ? 1 : 0;
