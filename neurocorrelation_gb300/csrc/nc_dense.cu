@@ -59,6 +59,18 @@ __device__ __forceinline__ void wait_previous_pass()
     if (NC_PDL) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// The synapse pass lets the neuron pass's blocks be scheduled once its own wait has
+// passed (so the neuron pass that follows cannot start before the one that preceded has
+// completed); the neuron pass then reads what no synapse pass writes (step counters, last
+// fires, potentials, row bounds, input draws) before its own wait.
+#ifndef NC_NEURON_EARLY_START
+#define NC_NEURON_EARLY_START 1
+#endif
+__device__ __forceinline__ void release_next_pass()
+{
+    if (NC_PDL && NC_NEURON_EARLY_START) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ int warp_sum(int v)
 {
 #pragma unroll
@@ -513,6 +525,7 @@ __global__ void __launch_bounds__(32 * kStageWarps, NC_STAGE_MIN_BLOCKS) k_dense
     WarpStage& ws = reinterpret_cast<WarpStage*>(dyn_smem)[threadIdx.x >> 5];
     init_stages(ws, threadIdx.x & 31);
     wait_previous_pass();
+    release_next_pass();
     uint32_t phases = 0u;  // bit j: parity of slot j's next completion
     synapse_pass<kFlush>(P, ws, sh, phases);
 }
@@ -654,6 +667,9 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
                 }
             }
         }
+        // everything above reads state no synapse pass writes; the folds and the update
+        // below need the synapse pass of this step
+        if (NC_NEURON_EARLY_START) wait_previous_pass();
         if (NC_FOLD_PACK) {
             const uint32_t need_m = __ballot_sync(kFull, need);
             if (lane == 0) s_cnt[wib] = __popc(need_m);
@@ -747,6 +763,8 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
             }
         }
     }
+    // (a block with no tile of its own still waits before the step counters can move)
+    if (NC_NEURON_EARLY_START) wait_previous_pass();
     block_counters<1>(P, s_net, sh.s_acc, wib, lane, acc_net, acc, 0);
     // the last block to finish advances the step counters
     __threadfence();
@@ -771,7 +789,7 @@ __device__ __forceinline__ void neuron_pass(const NcPools& P, PassShared& sh)
 __global__ void __launch_bounds__(NC_DNEURON_MAXT, NC_DNEURON_MINB) k_dense_neurons(NcPools P)
 {
     __shared__ PassShared sh;
-    wait_previous_pass();
+    if (!NC_NEURON_EARLY_START) wait_previous_pass();
     neuron_pass(P, sh);
 }
 
