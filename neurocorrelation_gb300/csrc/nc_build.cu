@@ -437,6 +437,9 @@ int build_knn_device(int32_t n, int32_t k, float density, uint64_t seed, const n
     NetHost& h = net->host;
     int rc = build_net(n, xyz.data(), 0, nullptr, nullptr, nullptr, nullptr, nullptr, p, h, err);
     if (rc != NC_OK) return rc;
+    // h.nonneg_terms stays true: the weights written below are in [0, 1) and no synapse is
+    // inhibitory, so no term of this network can be negative
+    h.nonneg_terms = true;
     // in-degrees by target slot -> row starts
     int32_t* d_slot = dalloc<int32_t>((size_t)n, own.v, e);
     int32_t* d_deg = dalloc<int32_t>((size_t)n, own.v, e);
